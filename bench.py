@@ -1,0 +1,387 @@
+"""Benchmark: plane-wave H.psi band-applications/s on one GB300 (mixed and FP64).
+
+Workload (default ``si64``): 64-atom Si cube, side 20.52 bohr, Ecut 20 Ha
+(37,073 plane waves), 96^3 FFT grid, Gamma point, 160 bands applied in blocks of
+32, 256 projectors (s + p on every atom).  One step = H.psi (kinetic + local
+potential + nonlocal) on all 160 bands.  Inputs are seeded synthetic data of
+that shape (qimpy_gb300.workloads), resident in HBM before the timed region.
+
+Precision forms:
+  mixed - complex64 wavefunctions, FP32 FFTs and GEMMs (the headline `value`)
+  fp64  - complex128 throughout, the plain drop-in form (reported in `fp64`)
+
+Timing: W warm-up steps, then K steps, each bracketed by CUDA events on the
+launching stream with a 512 MB L2 flush between steps (outside the events);
+N > 1 GPUs (torchrun) run independent replicas ("replicas only": H.psi has no
+exchange step), value = bands of all ranks / max-over-ranks time.
+
+`--impl reference` times the CPU oracle (the reference's FP64 algorithm restated
+with numpy/scipy, all host threads) on a bounded band sample of the same
+workload and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H.psi band-applications/s"
+UNIT = "band-applications/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="si64")
+    ap.add_argument("--cpu-sample-bands", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# Distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+
+
+def dist_init():
+    import torch
+
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, ws, local
+
+
+def dist_max(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ---------------------------------------------------------------------------
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms in a background process."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# Workload
+# ---------------------------------------------------------------------------
+
+
+def make_workload(name: str):
+    from qimpy_gb300 import workloads as wl
+
+    p = wl.get(name)
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape)
+    beta = wl.make_projectors(p, b)
+    nb = p.n_bands
+    C = wl.make_wavefunctions(p, b, nb)
+    return p, b, beta, C
+
+
+def roofline_counts(p, b, tables, nb_tile: int, real_bytes: int):
+    """Algorithmic bytes and flops per band-application."""
+    N = int(np.prod(p.grid_shape))
+    n = float(b.n.mean())
+    P = p.n_projectors
+    s_c = 2 * real_bytes
+    log2N = np.log2(N)
+    flops_loc = 2 * 5 * N * log2N + 2 * N + 2 * n
+    flops_nl = 2 * 8 * P * n + 8 * P * p.p_atom
+    bytes_loc = 2 * n * s_c + (N * real_bytes + n * 4) / nb_tile
+    bytes_nl = 2 * n * s_c + 2 * P * n * s_c / nb_tile
+    return dict(flops_loc=flops_loc, flops_nl=flops_nl, bytes_loc=bytes_loc, bytes_nl=bytes_nl)
+
+
+def measure_fma_peak(dtype_code: int) -> float:
+    """FP64 / FP32 CUDA-core FMA peak in TFLOP/s (best of 5)."""
+    import torch
+
+    from qimpy_gb300 import _lib
+
+    lib = _lib.lib()
+    blocks, threads, iters = 152 * 8, 256, 4096
+    out = torch.empty(blocks, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        _lib.check(lib.qgb_fma_burn(dtype_code, blocks, threads, iters, out.data_ptr(), st.cuda_stream), "fma")
+        e1.record(st)
+        e1.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3
+        best = max(best, blocks * threads * iters * 128 / sec / 1e12)
+    return best
+
+
+def run_gb300(args, rank, ws, local):
+    import torch
+
+    from qimpy_gb300 import _lib, ops, sphere as sp
+
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    p, b, beta_np, C_np = make_workload(args.workload)
+    tables = sp.build_tables(b.fft_index, b.n, p.grid_shape)
+    nb = C_np.shape[1]
+    block = p.block_size or nb
+    blocks = [(s, min(s + block, nb)) for s in range(0, nb, block)]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    results = {}
+    for form, cdt in (("fp64", torch.complex128), ("mixed", torch.complex64)):
+        ds = sp.DeviceSphere(tables, b.ke, dev, cdt)
+        ds.set_potential(torch.from_numpy(p.V_r))
+        C = torch.from_numpy(C_np).to(dev, cdt)
+        beta = torch.from_numpy(beta_np).to(dev, cdt)
+        D = torch.from_numpy(p.D_atom).to(dev, cdt)
+        HC = torch.empty_like(C)
+        projT = torch.empty((p.nk, block, p.n_projectors), dtype=cdt, device=dev)
+        work = torch.empty_like(projT)
+        wsp = ops.workspace(ds.workspace_bytes(block), dev)
+        st = torch.cuda.current_stream()
+
+        C_blk = [C[:, s0:s1].contiguous() for (s0, s1) in blocks]
+        H_blk = [torch.empty_like(c) for c in C_blk]
+
+        def step(ev=None):
+            for j, (s0, s1) in enumerate(blocks):
+                Cb, Hb = C_blk[j], H_blk[j]
+                if ev is not None:
+                    ev[0].record(st)
+                ops.apply_potential(ds, Cb, out=Hb, add_ke=True, ws=wsp)
+                if ev is not None:
+                    ev[1].record(st)
+                pT = projT[:, : s1 - s0]
+                ops.project(beta, Cb, pT)
+                ops.apply_nonlocal(beta, D, pT, Hb, work[:, : s1 - s0])
+                if ev is not None:
+                    ev[2].record(st)
+                    ev = ev[3:]
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        dist_barrier(ws)
+        clock = ClockSampler(local)
+        if form == "mixed":
+            clock.start()
+        times, t_loc, t_nl = [], [], []
+        for _ in range(args.steps):
+            flush.zero_()
+            evs = [torch.cuda.Event(enable_timing=True) for _ in range(3 * len(blocks))]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            step(evs)
+            e1.record(st)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+            for j in range(len(blocks)):
+                t_loc.append(evs[3 * j].elapsed_time(evs[3 * j + 1]) * 1e-3)
+                t_nl.append(evs[3 * j + 1].elapsed_time(evs[3 * j + 2]) * 1e-3)
+        clocks = clock.stop() if form == "mixed" else None
+        HC = torch.cat(H_blk, dim=1)
+        dist_barrier(ws)
+        total = dist_max(float(np.sum(times)), ws)
+        res = dict(value=nb * p.nk * args.steps * ws / total, ms_per_step=1e3 * total / args.steps,
+                   t_loc_block=float(np.median(t_loc)), t_nl_block=float(np.median(t_nl)),
+                   clocks=clocks)
+        # End-to-end through the public API with host buffers (pinned), every step.
+        if not args.no_e2e:
+            Ch = torch.from_numpy(C_np).to(cdt).pin_memory()
+            Hh = torch.empty_like(Ch).pin_memory()
+            def e2e_step():
+                Cd = Ch.to(dev, non_blocking=True)
+                for (s0, s1) in blocks:
+                    Hb, _ = ops.hamiltonian(ds, Cd[:, s0:s1].contiguous(), beta, D)
+                    Hh[:, s0:s1].copy_(Hb, non_blocking=True)
+            for _ in range(max(1, args.warmup)):
+                e2e_step()
+            torch.cuda.synchronize()
+            e2e_times = []
+            for _ in range(args.steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                e2e_step()
+                e1.record(st)
+                torch.cuda.synchronize()
+                e2e_times.append(e0.elapsed_time(e1) * 1e-3)
+            tot = dist_max(float(np.sum(e2e_times)), ws)
+            nbytes = Ch.numel() * Ch.element_size()
+            res["e2e"] = dict(value=nb * p.nk * args.steps * ws / tot, unit=UNIT, h2d_bytes_per_step=nbytes,
+                              d2h_bytes_per_step=nbytes)
+            err = float((Hh.to(dev) - HC).abs().max() / HC.abs().max())
+            res["e2e_matches_device_result"] = err
+        res["launches_per_step"] = 3 * len(blocks)  # our kernels; cuBLAS GEMMs are library calls
+        res["real_bytes"] = 8 if cdt == torch.complex128 else 4
+        res["block"] = block
+        results[form] = res
+        del ds, C, beta, HC, wsp
+        torch.cuda.empty_cache()
+    peaks = {"fp64": measure_fma_peak(_lib.QGB_F64), "fp32": measure_fma_peak(_lib.QGB_F32)}
+    return p, b, tables, results, peaks
+
+
+def cpu_baseline(args, p=None, b=None, beta=None, C=None, threads=None):
+    """Oracle H.psi (FP64, numpy/scipy) on a bounded band sample, timed on host cores."""
+    from oracle import hpsi as oh
+
+    threads = threads or os.cpu_count()
+    oh.set_threads(threads)
+    if p is None:
+        p, b, beta, C = make_workload(args.workload)
+    nbs = max(1, args.cpu_sample_bands)
+    Cs = C[:, :nbs]
+    D = p.D_all()
+    oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, D, Cs)  # warm-up
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, D, Cs)
+        reps += 1
+        if time.perf_counter() - t0 > 10.0 or reps >= 20:
+            break
+    sec = (time.perf_counter() - t0) / reps
+    return dict(value=nbs * p.nk / sec, unit=UNIT, cores=threads, kind="port",
+                sample=f"{nbs} bands x {p.nk} k of {args.workload}, {reps} H.psi calls, scipy.fft workers={threads}")
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        if rank != 0:
+            return
+        cb = cpu_baseline(args)
+        out = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
+               "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+               "dtype": "f64", "data": "synthetic", "config": {"workload": args.workload},
+               "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                           "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+    rank, ws, local = dist_init()
+    p, b, tables, results, peaks = run_gb300(args, rank, ws, local)
+    mixed, f64 = results["mixed"], results["fp64"]
+    # Roofline of the dominant stage of the mixed form (local potential, 3 kernels).
+    rc = roofline_counts(p, b, tables, mixed["block"], mixed["real_bytes"])
+    band_apps_block = mixed["block"] * p.nk
+    t_loc = mixed["t_loc_block"]
+    import json as _j
+
+    peaks_file = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak = _j.load(open(peaks_file))["hbm_gbs"] if os.path.exists(peaks_file) else 6800.0
+    ach_gbs = rc["bytes_loc"] * band_apps_block / t_loc / 1e9
+    ach_tflops = rc["flops_loc"] * band_apps_block / t_loc / 1e12
+    out = {
+        "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (f32)", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: 64-atom Si, 96^3 grid, n=37073, Gamma, 160 bands in blocks of 32, P=256",
+                   "l2": "flushed (512 MB write) between timed steps", "parallelism": f"replicas x{ws}"},
+        "fp64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"], "e2e": f64.get("e2e")},
+        "mixed_over_fp64": mixed["value"] / f64["value"],
+        "e2e": mixed.get("e2e"),
+        "stages_ms_per_block": {"mixed": {"local": 1e3 * mixed["t_loc_block"], "nonlocal": 1e3 * mixed["t_nl_block"]},
+                                "fp64": {"local": 1e3 * f64["t_loc_block"], "nonlocal": 1e3 * f64["t_nl_block"]}},
+        "roofline": {"kernel": "apply_potential (k_ifft_yz + k_xpass + k_fft_yz_gather), mixed",
+                     "bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": ach_gbs / hbm_peak, "traffic": None,
+                     "fp32": {"achieved_tflops": ach_tflops, "peak_tflops": peaks["fp32"],
+                              "frac": ach_tflops / peaks["fp32"]}},
+        "measured_fma_peaks_tflops": peaks,
+        "gpu_launches": mixed["launches_per_step"] * args.steps,
+        "clocks": mixed["clocks"],
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/*
+ * qimpy_gb300: GB300 (sm_103a) plane-wave Hamiltonian apply for QimPy's eigensolvers.
+ *
+ * Plain C ABI.  Every pointer argument is a device pointer unless stated
+ * otherwise; complex arrays are interleaved (re, im) like C99 `double complex`
+ * / torch complex128 (QGB_F64) or `float complex` / complex64 (QGB_F32).
+ * Every call is asynchronous on `stream` (a cudaStream_t passed as void*;
+ * NULL = legacy default stream), performs no host synchronisation and no
+ * device allocation, and returns 0 on success or a QGB_ERR_* code; the text
+ * of the last error on the calling thread is returned by qgb_last_error().
+ *
+ * Array layouts (the reference's Wavefunction.coeff (spin, k, band, spinor,
+ * basis) with the singleton spin and spinor axes dropped):
+ *   C, HC   [nk][nb][n_tot]      wavefunction coefficients, padded basis
+ *   beta    [nk][P][n_tot]       projectors beta_p(k+G); padding must be zero
+ *   projT   [nk][nb][P]          projections <beta_p|psi_b> (band-major)
+ *   D       [n_atoms][pa][pa]    per-atom blocks of the block-diagonal D_all,
+ *                                row-major, complex, P = n_atoms * pa
+ * Input wavefunctions must have zero padding (entries g >= n[k]), the
+ * invariant Wavefunction.constrain() keeps in the reference
+ * (qimpy/dft/electrons/_wavefunction.py:264-275); outputs always have zero padding.
+ */
+#ifndef QIMPY_GB300_H
+#define QIMPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QGB_ABI_VERSION 1
+
+enum qgb_dtype { QGB_F64 = 0, QGB_F32 = 1 };
+
+enum qgb_status {
+  QGB_OK = 0,
+  QGB_ERR_INVALID = 1,     /* bad argument: null pointer, size, unsupported grid */
+  QGB_ERR_WORKSPACE = 2,   /* workspace smaller than qgb_*_workspace_bytes() */
+  QGB_ERR_CUDA = 3,        /* CUDA runtime or launch error */
+  QGB_ERR_CUBLAS = 4,      /* cuBLAS error */
+  QGB_ERR_UNSUPPORTED = 5  /* valid request this build does not implement */
+};
+
+/* Flags of qgb_apply_potential. */
+#define QGB_ADD_KE 1u       /* out = KE*C + V*C instead of V*C */
+#define QGB_ACCUMULATE 2u   /* out += ... instead of out = ... */
+
+/*
+ * G-sphere layout of one basis (all k-points of a cell) on the FFT grid
+ * N0 x N1 x N2 (N2 fastest).  Built once per basis by the host from the
+ * reference's fft_index (qimpy/dft/electrons/_basis.py:186-193): in-sphere
+ * points are sorted by linear grid index, so the points with the same first
+ * grid index i0 (one "slab") are contiguous in the basis.
+ *
+ *   n[nk]                       in-sphere count per k
+ *   n_slabs[nk]                 number of distinct i0 values touched per k
+ *   slab_start[nk][max_slabs+1] basis offset of each slab (last = n[k])
+ *   slab_i0[nk][max_slabs]      i0 of each slab
+ *   yz[nk][n_tot]               packed (i1 << 16) | i2 of each in-sphere point
+ *   row_start[nk][max_slabs+1]  offsets into `rows` of each slab's active i1 list
+ *   rows[...]                   distinct i1 values of each slab (z-FFT pencils)
+ *   twiddle_{f64,f32}           per axis a, L1[a]*L2[a] complex values
+ *                               exp(+2 pi i n1 k2 / N_a), n1 < L1[a], k2 < L2[a],
+ *                               axis 0 first; offsets tw_off[a]
+ *   ke                          [nk][n_tot] kinetic energy, 0.5 |k+G|^2 (real,
+ *                               of the call's dtype)
+ *   V                           [N0][N1][N2] real potential in the digit-permuted
+ *                               real-space order of qgb_permute_real_space()
+ */
+typedef struct qgb_sphere {
+  int32_t nk, n_tot;
+  int32_t N[3];
+  int32_t L1[3], L2[3];     /* N[a] = L1[a] * L2[a]; both in {1..10,12,14,15,16} */
+  int32_t max_slabs, max_rows;
+  int32_t tw_off[3];
+  const int32_t* n;
+  const int32_t* n_slabs;
+  const int32_t* slab_start;
+  const int32_t* slab_i0;
+  const int32_t* yz;
+  const int32_t* row_start;
+  const int32_t* rows;
+  const void* twiddle;      /* complex of the call's dtype */
+  const void* ke;           /* real of the call's dtype */
+  const void* V;            /* real of the call's dtype, permuted order */
+} qgb_sphere;
+
+/* Library identification. */
+int qgb_abi_version(void);
+const char* qgb_last_error(void);
+
+/*
+ * Workspace (bytes) that qgb_apply_potential / qgb_hamiltonian need for `nb`
+ * bands; any size >= 1 slab-plane per band chunk works, larger sizes let more
+ * bands run per launch.  Host function, no device access.
+ */
+size_t qgb_potential_workspace_bytes(const qgb_sphere* s, int nb, int dtype);
+
+/*
+ * Real-space permutation used for V: position p along axis a holds real-space
+ * index perm[a][p] = (p / L1) + L2 * (p % L1).  Host function; writes N[a]
+ * entries per axis into host array perm (axis 0, then 1, then 2).
+ */
+int qgb_permute_real_space(const qgb_sphere* s, int32_t* perm);
+
+/*
+ * out[k][b] = KE[k] * C[k][b]  (replaces Basis.apply_ke,
+ * qimpy/dft/electrons/_basis_ops.py:29-36).
+ */
+int qgb_apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, void* stream);
+
+/*
+ * out = gather(FFT(V * IFFT(scatter(C)))) for nb bands at every k of the sphere
+ * (replaces Basis.apply_potential for one spin channel,
+ * qimpy/dft/electrons/_basis_ops.py:39-113 with _ApplyPotentialKernel 166-204):
+ * inverse FFT unnormalised, forward FFT scaled by 1/(N0 N1 N2), padding zeroed.
+ * flags: QGB_ADD_KE adds KE*C (fusing Basis.apply_ke), QGB_ACCUMULATE adds into out.
+ * `workspace` holds intermediate slab planes (qgb_potential_workspace_bytes).
+ */
+int qgb_apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb,
+                        unsigned flags, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * projT[k][b][p] = sum_g conj(beta[k][p][g]) C[k][b][g]  (replaces Wavefunction.proj
+ * = beta ^ C, qimpy/dft/electrons/_wavefunction.py:106-123 and
+ * _wavefunction_dot.py:18-107).
+ */
+int qgb_project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb,
+                int n_tot, void* stream);
+
+/*
+ * out[k][b][g] += sum_p beta[k][p][g] (D_all projT[k][b])[p]  (replaces
+ * beta @ (D_all @ C.proj), qimpy/dft/electrons/_hamiltonian.py:22-24 with
+ * Wavefunction.matmul, _wavefunction_dot.py:137-191).  D is given per atom
+ * block (n_atoms blocks of pa x pa).  `work` holds nk*nb*P complex values.
+ */
+int qgb_apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int pa,
+                       const void* projT, void* out, int nk, int nb, int n_tot, void* work,
+                       void* stream);
+
+/*
+ * HC = KE C + V C + beta D <beta|C>  (replaces Electrons.hamiltonian,
+ * qimpy/dft/electrons/_hamiltonian.py:7-29, for a fixed local potential).
+ * projT receives <beta|C> (the reference caches it as C.proj).  Workspace:
+ * qgb_potential_workspace_bytes + nk*nb*P complex values.  beta may be NULL
+ * when P == 0.
+ */
+int qgb_hamiltonian(const qgb_sphere* s, int dtype, const void* C, void* HC, int nb,
+                    const void* beta, const void* D, int n_atoms, int pa, void* projT,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int dtype);
+
+/*
+ * Diagnostic: `blocks` x `threads` threads each run 8 independent FMA chains
+ * for 8*iters steps (16*iters flops per thread) in the given dtype.  Timed by
+ * the caller; gives the FP64/FP32 CUDA-core peak used as a roofline
+ * denominator.  `out` receives nothing in practice (needs `blocks` reals).
+ * No reference counterpart (measurement aid).
+ */
+int qgb_fma_burn(int dtype, int blocks, int threads, int iters, void* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QIMPY_GB300_H */

@@ -1,0 +1,77 @@
+"""FP64 CPU restatement of the reference's Hamiltonian apply (test infrastructure only).
+
+Layouts follow the reference with the singleton spin and spinor axes dropped:
+coefficients C[k, b, g] complex128 with g over the padded basis n_tot,
+projectors beta[k, p, g], projections proj[k, p, b], D_all[p, p'].
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import scipy.fft as sfft
+
+_WORKERS = int(os.environ.get("ORACLE_THREADS", "1"))
+
+
+def set_threads(n: int) -> None:
+    """Threads used by the FFTs of the oracle (1 = scalar port)."""
+    global _WORKERS
+    _WORKERS = max(1, int(n))
+
+
+def constrain(C: np.ndarray, n: np.ndarray) -> np.ndarray:
+    """Zero padded coefficients beyond n[k] (qimpy/dft/electrons/_wavefunction.py:264-275)."""
+    for k in range(C.shape[0]):
+        C[k, ..., int(n[k]) :] = 0.0
+    return C
+
+
+def apply_ke(ke: np.ndarray, C: np.ndarray) -> np.ndarray:
+    """KE(k, g) * C (qimpy/dft/electrons/_basis_ops.py:29-36; KE from _basis.py:256-270)."""
+    return C * ke[:, None, :]
+
+
+def apply_potential(V_r: np.ndarray, fft_index: np.ndarray, n: np.ndarray, C: np.ndarray) -> np.ndarray:
+    """gather(fft(V * ifft(scatter(C)))) then zero padding.
+
+    Follows qimpy/dft/electrons/_basis_ops.py:39-113 and 152-199: scatter every
+    padded coefficient to its grid point (fft_index), inverse FFT with
+    norm="forward" (no scaling; qimpy/grid/_fft.py:298), multiply by the real
+    V(r), forward FFT with norm="forward" (scale 1/N; qimpy/grid/_fft.py:239),
+    gather at fft_index, then ``constrain``."""
+    nk, nb, n_tot = C.shape
+    shape = V_r.shape
+    N = int(np.prod(shape))
+    out = np.empty_like(C)
+    for k in range(nk):
+        grid = np.zeros((nb, N), dtype=np.complex128)
+        grid[:, fft_index[k]] = C[k]
+        psi_r = sfft.ifftn(grid.reshape((nb,) + shape), axes=(1, 2, 3), norm="forward", workers=_WORKERS)
+        psi_r *= V_r[None]
+        VC = sfft.fftn(psi_r, axes=(1, 2, 3), norm="forward", workers=_WORKERS).reshape(nb, N)
+        out[k] = VC[:, fft_index[k]]
+    return constrain(out, n)
+
+
+def project(beta: np.ndarray, C: np.ndarray) -> np.ndarray:
+    """<beta|C>: proj[k, p, b] = sum_g conj(beta[k, p, g]) C[k, b, g]
+    (qimpy/dft/electrons/_wavefunction.py:106-123 via _wavefunction_dot.py:18-107)."""
+    return np.matmul(beta.conj(), np.swapaxes(C, 1, 2))
+
+
+def apply_nonlocal(beta: np.ndarray, D_all: np.ndarray, proj: np.ndarray) -> np.ndarray:
+    """beta @ (D_all @ proj): out[k, b, g] = sum_p beta[k, p, g] (D proj)[k, p, b]
+    (qimpy/dft/electrons/_hamiltonian.py:22-24; matmul of _wavefunction_dot.py:137-191)."""
+    Dp = np.matmul(D_all[None], proj)
+    return np.matmul(np.swapaxes(Dp, 1, 2), beta)
+
+
+def hamiltonian(ke, V_r, fft_index, n, beta, D_all, C) -> np.ndarray:
+    """HC = KE C + V C + beta D <beta|C> (qimpy/dft/electrons/_hamiltonian.py:7-29;
+    the meta-GGA tau and DFT+U terms are absent for a fixed LDA-like potential)."""
+    HC = apply_ke(ke, C)
+    HC += apply_potential(V_r, fft_index, n, C)
+    if beta is not None and beta.shape[1]:
+        HC += apply_nonlocal(beta, D_all, project(beta, C))
+    return HC

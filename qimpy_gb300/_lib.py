@@ -1,0 +1,92 @@
+"""ctypes binding of ``libqimpy_gb300.so`` (the C ABI of include/qimpy_gb300.h).
+
+The library is loaded from the package directory only; there is no fallback:
+if it is missing, every GPU operation raises.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import threading
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libqimpy_gb300.so")
+
+QGB_F64, QGB_F32 = 0, 1
+QGB_ADD_KE, QGB_ACCUMULATE = 1, 2
+ABI_VERSION = 1
+
+_ERRORS = {1: "invalid argument", 2: "workspace too small", 3: "CUDA error", 4: "cuBLAS error",
+           5: "unsupported"}
+
+
+class QgbSphere(ct.Structure):
+    """Mirror of ``struct qgb_sphere``."""
+
+    _fields_ = [
+        ("nk", ct.c_int32), ("n_tot", ct.c_int32),
+        ("N", ct.c_int32 * 3), ("L1", ct.c_int32 * 3), ("L2", ct.c_int32 * 3),
+        ("max_slabs", ct.c_int32), ("max_rows", ct.c_int32), ("tw_off", ct.c_int32 * 3),
+        ("n", ct.c_void_p), ("n_slabs", ct.c_void_p), ("slab_start", ct.c_void_p),
+        ("slab_i0", ct.c_void_p), ("yz", ct.c_void_p), ("row_start", ct.c_void_p),
+        ("rows", ct.c_void_p), ("twiddle", ct.c_void_p), ("ke", ct.c_void_p), ("V", ct.c_void_p),
+    ]
+
+
+class QgbError(RuntimeError):
+    """Nonzero status returned by the library."""
+
+
+_lock = threading.Lock()
+_lib = None
+
+_SIGS = {
+    "qgb_abi_version": (ct.c_int, []),
+    "qgb_last_error": (ct.c_char_p, []),
+    "qgb_potential_workspace_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int, ct.c_int]),
+    "qgb_hamiltonian_workspace_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int, ct.c_int, ct.c_int]),
+    "qgb_permute_real_space": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_void_p]),
+    "qgb_apply_ke": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p]),
+    "qgb_apply_potential": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
+                                       ct.c_uint, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_project": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int,
+                               ct.c_int, ct.c_void_p]),
+    "qgb_apply_nonlocal": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p,
+                                      ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "qgb_hamiltonian": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
+                                   ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                   ct.c_size_t, ct.c_void_p]),
+    "qgb_fma_burn": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
+}
+
+#: Every symbol the header declares (checked by the CPU tests).
+EXPORTED = tuple(_SIGS)
+
+
+def lib() -> ct.CDLL:
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not os.path.exists(LIB_PATH):
+                    raise RuntimeError(
+                        f"{LIB_PATH} is missing: build it with `python -m qimpy_gb300.build` "
+                        "(the CUDA extension is required; there is no CPU fallback)"
+                    )
+                handle = ct.CDLL(LIB_PATH)
+                for name, (res, args) in _SIGS.items():
+                    fn = getattr(handle, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                if handle.qgb_abi_version() != ABI_VERSION:
+                    raise RuntimeError("libqimpy_gb300.so ABI version mismatch; rebuild it")
+                _lib = handle
+    return _lib
+
+
+def check(status: int, what: str) -> None:
+    """Raise QgbError with the library's message for a nonzero status."""
+    if status != 0:
+        msg = lib().qgb_last_error().decode(errors="replace")
+        raise QgbError(f"{what}: {_ERRORS.get(status, status)}: {msg}")

@@ -1,0 +1,122 @@
+// extern "C" entry points of libqimpy_gb300 (declared in include/qimpy_gb300.h).
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "qgb_common.cuh"
+
+namespace qgb {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int validate_sphere(const qgb_sphere* s, int dtype);
+size_t plane_bytes_per_band(const qgb_sphere& s, int dtype);
+int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
+                    void* ws, size_t ws_bytes, cudaStream_t st);
+int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, cudaStream_t st);
+int project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb, int n_tot,
+            cudaStream_t st);
+int apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int pa, const void* projT,
+                   void* out, int nk, int nb, int n_tot, void* work, cudaStream_t st);
+
+}  // namespace qgb
+
+using namespace qgb;
+
+extern "C" {
+
+int qgb_abi_version(void) { return QGB_ABI_VERSION; }
+
+const char* qgb_last_error(void) { return g_last_error.c_str(); }
+
+size_t qgb_potential_workspace_bytes(const qgb_sphere* s, int nb, int dtype) {
+  if (!s || nb < 0) return 0;
+  return plane_bytes_per_band(*s, dtype) * static_cast<size_t>(nb);
+}
+
+size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int dtype) {
+  if (!s || nb < 0 || P < 0) return 0;
+  const size_t nl = static_cast<size_t>(s->nk) * nb * P * elem_bytes(dtype);
+  const size_t nl_aligned = (nl + 255) / 256 * 256;
+  return nl_aligned + plane_bytes_per_band(*s, dtype) * static_cast<size_t>(nb);
+}
+
+int qgb_permute_real_space(const qgb_sphere* s, int32_t* perm) {
+  if (!s || !perm) return fail(QGB_ERR_INVALID, "NULL argument");
+  int off = 0;
+  for (int a = 0; a < 3; ++a) {
+    const int L1 = s->L1[a], L2 = s->L2[a];
+    if (L1 < 1 || L2 < 1 || L1 * L2 != s->N[a]) return fail(QGB_ERR_INVALID, "bad factorisation on axis %d", a);
+    for (int p = 0; p < s->N[a]; ++p) perm[off + p] = p / L1 + L2 * (p % L1);
+    off += s->N[a];
+  }
+  return QGB_OK;
+}
+
+int qgb_apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, void* stream) {
+  return apply_ke(s, dtype, C, out, nb, static_cast<cudaStream_t>(stream));
+}
+
+int qgb_apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  return apply_potential(s, dtype, C, out, nb, flags, workspace, workspace_bytes,
+                         static_cast<cudaStream_t>(stream));
+}
+
+int qgb_project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb, int n_tot,
+                void* stream) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
+  return project(dtype, beta, C, projT, nk, P, nb, n_tot, static_cast<cudaStream_t>(stream));
+}
+
+int qgb_apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int pa, const void* projT,
+                       void* out, int nk, int nb, int n_tot, void* work, void* stream) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
+  return apply_nonlocal(dtype, beta, D, n_atoms, pa, projT, out, nk, nb, n_tot, work,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int qgb_hamiltonian(const qgb_sphere* s, int dtype, const void* C, void* HC, int nb, const void* beta,
+                    const void* D, int n_atoms, int pa, void* projT, void* workspace,
+                    size_t workspace_bytes, void* stream) {
+  int rc = validate_sphere(s, dtype);
+  if (rc) return rc;
+  if (C == HC) return fail(QGB_ERR_INVALID, "C and HC must not alias");
+  const int P = n_atoms * pa;
+  const size_t nl = static_cast<size_t>(s->nk) * nb * P * elem_bytes(dtype);
+  const size_t nl_aligned = (nl + 255) / 256 * 256;
+  if (workspace_bytes < nl_aligned) return fail(QGB_ERR_WORKSPACE, "workspace too small for nonlocal term");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* ws = static_cast<char*>(workspace);
+  rc = apply_potential(s, dtype, C, HC, nb, QGB_ADD_KE, ws + nl_aligned, workspace_bytes - nl_aligned, st);
+  if (rc) return rc;
+  if (P > 0) {
+    if (!projT) return fail(QGB_ERR_INVALID, "projT is NULL with P > 0");
+    rc = project(dtype, beta, C, projT, s->nk, P, nb, s->n_tot, st);
+    if (rc) return rc;
+    rc = apply_nonlocal(dtype, beta, D, n_atoms, pa, projT, HC, s->nk, nb, s->n_tot, ws, st);
+    if (rc) return rc;
+  }
+  return QGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,387 @@
+// Local-potential apply V*psi on the G-sphere: scatter -> 3D inverse FFT -> *V(r)
+// -> 3D forward FFT -> gather (+ KE*psi), for a block of bands at every k.
+//
+// Replaces Basis.apply_potential (qimpy/dft/electrons/_basis_ops.py:39-113, with
+// _KernelCommon.expand_ifft 152-163 and _ApplyPotentialKernel.__call__ 183-199)
+// and fuses Basis.apply_ke (_basis_ops.py:29-36).  FFT conventions follow
+// qimpy/grid/_fft.py: inverse unnormalised, forward scaled by 1/N.
+//
+// The 3D transform is split by the G-sphere's structure.  In-sphere points are
+// sorted by linear grid index, so each "slab" (points sharing the first grid
+// index i0) is a contiguous range of the basis, and only the n_slabs i0 values
+// the sphere touches carry data:
+//   k_ifft_yz      one CTA per (k, band, slab): scatter the slab's points into
+//                  an N1 x N2 plane in shared memory, inverse z-FFT on the rows
+//                  the sphere touches, inverse y-FFT on all columns, store the
+//                  plane (real-space y, z in permuted order) to the workspace.
+//   k_xpass        one CTA per (k, band, y-row): gather the slabs' rows into
+//                  N2 pencils along x, inverse x-FFT, multiply by V(r), forward
+//                  x-FFT, keep only the slab rows, store back.
+//   k_fft_yz_gather one CTA per (k, band, slab): forward y-FFT on all columns,
+//                  forward z-FFT on the touched rows, gather the slab's points,
+//                  scale by 1/N and add KE*psi.
+// Versus three full-grid passes each way this skips the empty x-planes in the
+// y/z passes and the empty z-rows in the z passes.
+#include <algorithm>
+
+#include "fft_steps.cuh"
+
+namespace qgb {
+
+static constexpr int kThreads = 256;
+
+struct LocalParams {
+  int nb_total;  // bands in C / out (stride of the band axis)
+  int b0;        // first band of this chunk
+  int nb;        // bands in this chunk
+  unsigned flags;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_twiddles(cplx_t<T>* dst, const cplx_t<T>* src, int count) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = src[i];
+}
+
+// Plane workspace index of (k, band-in-chunk, slab).
+__device__ __forceinline__ size_t plane_index(const qgb_sphere& s, int k, int b, int nb, int slab) {
+  return (static_cast<size_t>(k) * nb + b) * s.max_slabs + slab;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_ifft_yz(const qgb_sphere s, LocalParams lp,
+                                                      const cplx_t<T>* __restrict__ C,
+                                                      cplx_t<T>* __restrict__ planes) {
+  using C2 = cplx_t<T>;
+  const int slab = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
+  if (slab >= s.n_slabs[k]) return;
+  const int N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* P = reinterpret_cast<C2*>(smem_raw);
+  C2* Wy = P + N1 * ld;
+  C2* Wz = Wy + N1;
+  const C2* tw = static_cast<const C2*>(s.twiddle);
+  load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
+  load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
+  const C2 zero = mk<T>(T(0), T(0));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int r = warp; r < N1; r += nwarps)
+    for (int c = lane; c < N2; c += 32) P[r * ld + c] = zero;
+  __syncthreads();
+
+  // Scatter this slab's coefficients (contiguous in the basis) into the plane.
+  const int g0 = s.slab_start[k * (s.max_slabs + 1) + slab];
+  const int g1 = s.slab_start[k * (s.max_slabs + 1) + slab + 1];
+  const C2* Cb = C + (static_cast<size_t>(k) * lp.nb_total + lp.b0 + b) * s.n_tot;
+  const int* yz = s.yz + static_cast<size_t>(k) * s.n_tot;
+  for (int g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
+    const int v = yz[g];
+    P[(v >> 16) * ld + (v & 0xFFFF)] = Cb[g];
+  }
+  __syncthreads();
+
+  // Inverse z-FFT along the rows this slab touches (row stride ld, element stride 1).
+  const int r0 = s.row_start[k * (s.max_slabs + 1) + slab];
+  const int nrows = s.row_start[k * (s.max_slabs + 1) + slab + 1] - r0;
+  fft_inverse<T>(P, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz);
+  // Inverse y-FFT along all N2 columns (column stride 1, element stride ld).
+  fft_inverse<T>(P, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy);
+
+  C2* out = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
+  for (int r = warp; r < N1; r += nwarps)
+    for (int c = lane; c < N2; c += 32) out[r * N2 + c] = P[r * ld + c];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalParams lp,
+                                                    cplx_t<T>* __restrict__ planes) {
+  using C2 = cplx_t<T>;
+  const int r1 = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
+  const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
+  const int L1 = s.L1[0], L2 = s.L2[0];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* X = reinterpret_cast<C2*>(smem_raw);
+  C2* Wx = X + N0 * ld;
+  const C2* tw = static_cast<const C2*>(s.twiddle);
+  load_twiddles<T>(Wx, tw + s.tw_off[0], N0);
+  const C2 zero = mk<T>(T(0), T(0));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int r = warp; r < N0; r += nwarps)
+    for (int c = lane; c < N2; c += 32) X[r * ld + c] = zero;
+  __syncthreads();
+
+  const int nslabs = s.n_slabs[k];
+  const int* i0 = s.slab_i0 + k * s.max_slabs;
+  const size_t plane = static_cast<size_t>(N1) * N2;
+  C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2;
+  for (int sl = warp; sl < nslabs; sl += nwarps) {
+    const C2* src = base + sl * plane;
+    C2* dst = X + i0[sl] * ld;
+    for (int c = lane; c < N2; c += 32) dst[c] = src[c];
+  }
+  __syncthreads();
+
+  // Inverse x pass 1 (natural in).
+  if (L2 > 1) {
+    run_pass<T, +1>(L2, Pass<T>{X, nullptr, N2, 1, L1, ld, L1 * ld, Wx, L2, 1});
+    __syncthreads();
+  }
+  // Inverse pass 2, multiply by V at the permuted real-space position, forward
+  // pass A: the same thread owns block [L1 a, L1 a + L1) of a column in all three.
+  {
+    const T* V = static_cast<const T*>(s.V);
+    const int nitems = N2 * L2;
+    for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+      const int a = it / N2;
+      const int c = it - a * N2;
+      C2* p = X + c + a * L1 * ld;
+      const T* Vp = V + (static_cast<size_t>(a) * L1 * N1 + r1) * N2 + c;
+      // L1 is a codelet size; dispatch once per item.
+      switch (L1) {
+#define QGB_XMID(R)                                                                        \
+  case R: {                                                                                \
+    T re[R], im[R];                                                                        \
+    _Pragma("unroll") for (int j = 0; j < R; ++j) {                                        \
+      const C2 v = p[j * ld];                                                              \
+      re[j] = v.x;                                                                         \
+      im[j] = v.y;                                                                         \
+    }                                                                                      \
+    Codelet<R, +1>::run(re, im);                                                           \
+    _Pragma("unroll") for (int j = 0; j < R; ++j) {                                        \
+      const T vv = Vp[static_cast<size_t>(j) * N1 * N2];                                   \
+      re[j] *= vv;                                                                         \
+      im[j] *= vv;                                                                         \
+    }                                                                                      \
+    Codelet<R, -1>::run(re, im);                                                           \
+    if (L2 > 1) {                                                                          \
+      _Pragma("unroll") for (int j = 1; j < R; ++j) {                                      \
+        const C2 w = Wx[j * L2 + a];                                                       \
+        const T xr = re[j] * w.x + im[j] * w.y;                                            \
+        const T xi = im[j] * w.x - re[j] * w.y;                                            \
+        re[j] = xr;                                                                        \
+        im[j] = xi;                                                                        \
+      }                                                                                    \
+    }                                                                                      \
+    _Pragma("unroll") for (int j = 0; j < R; ++j) p[j * ld] = mk<T>(re[j], im[j]);         \
+  } break;
+        QGB_XMID(1)
+        QGB_XMID(2)
+        QGB_XMID(3)
+        QGB_XMID(4)
+        QGB_XMID(5)
+        QGB_XMID(6)
+        QGB_XMID(7)
+        QGB_XMID(8)
+        QGB_XMID(9)
+        QGB_XMID(10)
+        QGB_XMID(12)
+        QGB_XMID(14)
+        QGB_XMID(15)
+        QGB_XMID(16)
+#undef QGB_XMID
+        default: break;
+      }
+    }
+    __syncthreads();
+  }
+  // Forward pass B (natural out).
+  if (L2 > 1) {
+    run_pass<T, -1>(L2, Pass<T>{X, nullptr, N2, 1, L1, ld, L1 * ld, nullptr, 0, 0});
+    __syncthreads();
+  }
+  for (int sl = warp; sl < nslabs; sl += nwarps) {
+    C2* dst = base + sl * plane;
+    const C2* src = X + i0[sl] * ld;
+    for (int c = lane; c < N2; c += 32) dst[c] = src[c];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, LocalParams lp,
+                                                            const cplx_t<T>* __restrict__ C,
+                                                            cplx_t<T>* __restrict__ out,
+                                                            const cplx_t<T>* __restrict__ planes) {
+  using C2 = cplx_t<T>;
+  const int slab = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
+  const int nslabs = s.n_slabs[k];
+  C2* Ob = out + (static_cast<size_t>(k) * lp.nb_total + lp.b0 + b) * s.n_tot;
+  const bool accumulate = (lp.flags & QGB_ACCUMULATE) != 0;
+  if (slab == 0 && !accumulate) {  // zero the padding entries of this band
+    const int nk_in = s.n[k];
+    for (int g = nk_in + threadIdx.x; g < s.n_tot; g += blockDim.x) Ob[g] = mk<T>(T(0), T(0));
+  }
+  if (slab >= nslabs) return;
+  const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* P = reinterpret_cast<C2*>(smem_raw);
+  C2* Wy = P + N1 * ld;
+  C2* Wz = Wy + N1;
+  const C2* tw = static_cast<const C2*>(s.twiddle);
+  load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
+  load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const C2* in = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
+  for (int r = warp; r < N1; r += nwarps)
+    for (int c = lane; c < N2; c += 32) P[r * ld + c] = in[r * N2 + c];
+  __syncthreads();
+
+  fft_forward<T>(P, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy);
+  const int r0 = s.row_start[k * (s.max_slabs + 1) + slab];
+  const int nrows = s.row_start[k * (s.max_slabs + 1) + slab + 1] - r0;
+  fft_forward<T>(P, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz);
+
+  const int g0 = s.slab_start[k * (s.max_slabs + 1) + slab];
+  const int g1 = s.slab_start[k * (s.max_slabs + 1) + slab + 1];
+  const C2* Cb = C + (static_cast<size_t>(k) * lp.nb_total + lp.b0 + b) * s.n_tot;
+  const int* yz = s.yz + static_cast<size_t>(k) * s.n_tot;
+  const T invN = T(1) / (T(N0) * T(N1) * T(N2));
+  const bool add_ke = (lp.flags & QGB_ADD_KE) != 0;
+  const T* ke = static_cast<const T*>(s.ke) + static_cast<size_t>(k) * s.n_tot;
+  for (int g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
+    const int v = yz[g];
+    const C2 f = P[(v >> 16) * ld + (v & 0xFFFF)];
+    T xr = f.x * invN, xi = f.y * invN;
+    if (add_ke) {
+      const C2 c = Cb[g];
+      const T e = ke[g];
+      xr = e * c.x + xr;
+      xi = e * c.y + xi;
+    }
+    if (accumulate) {
+      const C2 o = Ob[g];
+      xr += o.x;
+      xi += o.y;
+    }
+    Ob[g] = mk<T>(xr, xi);
+  }
+}
+
+template <typename T>
+__global__ void k_apply_ke(const qgb_sphere s, int nb, const cplx_t<T>* __restrict__ C,
+                           cplx_t<T>* __restrict__ out) {
+  const size_t total = static_cast<size_t>(s.nk) * nb * s.n_tot;
+  const T* ke = static_cast<const T*>(s.ke);
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t g = i % s.n_tot;
+    const size_t k = i / (static_cast<size_t>(nb) * s.n_tot);
+    const T e = ke[k * s.n_tot + g];
+    const cplx_t<T> c = C[i];
+    out[i] = mk<T>(e * c.x, e * c.y);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+static bool codelet_size(int R) {
+  switch (R) {
+    case 1: case 2: case 3: case 4: case 5: case 6: case 7: case 8: case 9: case 10:
+    case 12: case 14: case 15: case 16:
+      return true;
+    default:
+      return false;
+  }
+}
+
+size_t plane_smem_bytes(const qgb_sphere& s, int dtype) {
+  const size_t e = elem_bytes(dtype);
+  const size_t yz = (static_cast<size_t>(s.N[1]) * (s.N[2] + 1) + s.N[1] + s.N[2]) * e;
+  const size_t x = (static_cast<size_t>(s.N[0]) * (s.N[2] + 1) + s.N[0]) * e;
+  return std::max(yz, x);
+}
+
+int validate_sphere(const qgb_sphere* s, int dtype) {
+  if (s == nullptr) return fail(QGB_ERR_INVALID, "sphere descriptor is NULL");
+  if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
+  if (s->nk < 1 || s->n_tot < 1 || s->max_slabs < 1)
+    return fail(QGB_ERR_INVALID, "empty sphere (nk=%d n_tot=%d max_slabs=%d)", s->nk, s->n_tot,
+                s->max_slabs);
+  for (int a = 0; a < 3; ++a) {
+    if (s->N[a] < 1 || s->N[a] > 65535)
+      return fail(QGB_ERR_INVALID, "grid dimension %d = %d out of range", a, s->N[a]);
+    if (!codelet_size(s->L1[a]) || !codelet_size(s->L2[a]) || s->L1[a] * s->L2[a] != s->N[a])
+      return fail(QGB_ERR_INVALID, "axis %d: N=%d is not L1*L2 with L1=%d, L2=%d codelet sizes",
+                  a, s->N[a], s->L1[a], s->L2[a]);
+  }
+  if (s->max_slabs > s->N[0]) return fail(QGB_ERR_INVALID, "max_slabs %d > N0", s->max_slabs);
+  if (!s->n || !s->n_slabs || !s->slab_start || !s->slab_i0 || !s->yz || !s->row_start ||
+      !s->rows || !s->twiddle || !s->ke || !s->V)
+    return fail(QGB_ERR_INVALID, "sphere descriptor has a NULL table");
+  if (plane_smem_bytes(*s, dtype) > 227 * 1024)
+    return fail(QGB_ERR_UNSUPPORTED, "grid %dx%dx%d needs %zu B of shared memory per plane (max 227 KB)",
+                s->N[0], s->N[1], s->N[2], plane_smem_bytes(*s, dtype));
+  return QGB_OK;
+}
+
+size_t plane_bytes_per_band(const qgb_sphere& s, int dtype) {
+  return static_cast<size_t>(s.nk) * s.max_slabs * s.N[1] * s.N[2] * elem_bytes(dtype);
+}
+
+template <typename T>
+static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* C, void* out,
+                        void* planes, cudaStream_t st, size_t smem) {
+  using C2 = cplx_t<T>;
+  const dim3 g1(s.max_slabs, lp.nb, s.nk);
+  k_ifft_yz<T><<<g1, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(C), static_cast<C2*>(planes));
+  QGB_LAUNCH_CHECK("k_ifft_yz");
+  const dim3 g2(s.N[1], lp.nb, s.nk);
+  k_xpass<T><<<g2, kThreads, smem, st>>>(s, lp, static_cast<C2*>(planes));
+  QGB_LAUNCH_CHECK("k_xpass");
+  k_fft_yz_gather<T><<<g1, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(C),
+                                                static_cast<C2*>(out), static_cast<const C2*>(planes));
+  QGB_LAUNCH_CHECK("k_fft_yz_gather");
+  return QGB_OK;
+}
+
+template <typename T>
+static int set_smem_limits(size_t smem) {
+  static size_t configured = 0;
+  if (smem <= configured) return QGB_OK;
+  QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  QGB_CUDA_CHECK(cudaFuncSetAttribute(k_fft_yz_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  configured = smem;
+  return QGB_OK;
+}
+
+int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb,
+                    unsigned flags, void* ws, size_t ws_bytes, cudaStream_t st) {
+  int rc = validate_sphere(s, dtype);
+  if (rc) return rc;
+  if (nb < 0) return fail(QGB_ERR_INVALID, "nb = %d < 0", nb);
+  if (nb == 0) return QGB_OK;
+  // C == out is allowed: every chunk reads its bands of C (k_ifft_yz, and the
+  // KE term in k_fft_yz_gather before the same thread stores) before writing them.
+  if (!C || !out) return fail(QGB_ERR_INVALID, "NULL wavefunction pointer");
+  const size_t per_band = plane_bytes_per_band(*s, dtype);
+  if (!ws || ws_bytes < per_band)
+    return fail(QGB_ERR_WORKSPACE, "workspace %zu B < %zu B needed for one band", ws_bytes, per_band);
+  const int chunk = static_cast<int>(std::min<size_t>(nb, std::min<size_t>(ws_bytes / per_band, 65535)));
+  const size_t smem = plane_smem_bytes(*s, dtype);
+  rc = (dtype == QGB_F64) ? set_smem_limits<double>(smem) : set_smem_limits<float>(smem);
+  if (rc) return rc;
+  for (int b0 = 0; b0 < nb; b0 += chunk) {
+    LocalParams lp{nb, b0, std::min(chunk, nb - b0), flags};
+    rc = (dtype == QGB_F64) ? launch_chunk<double>(*s, lp, C, out, ws, st, smem)
+                            : launch_chunk<float>(*s, lp, C, out, ws, st, smem);
+    if (rc) return rc;
+  }
+  return QGB_OK;
+}
+
+int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, cudaStream_t st) {
+  if (s == nullptr) return fail(QGB_ERR_INVALID, "sphere descriptor is NULL");
+  if (nb < 0 || !C || !out || !s->ke) return fail(QGB_ERR_INVALID, "bad apply_ke arguments");
+  if (nb == 0) return QGB_OK;
+  const size_t total = static_cast<size_t>(s->nk) * nb * s->n_tot;
+  const int blocks = static_cast<int>(std::min<size_t>((total + 255) / 256, 152 * 16));
+  if (dtype == QGB_F64)
+    k_apply_ke<double><<<blocks, 256, 0, st>>>(*s, nb, static_cast<const double2*>(C), static_cast<double2*>(out));
+  else
+    k_apply_ke<float><<<blocks, 256, 0, st>>>(*s, nb, static_cast<const float2*>(C), static_cast<float2*>(out));
+  QGB_LAUNCH_CHECK("k_apply_ke");
+  return QGB_OK;
+}
+
+}  // namespace qgb

@@ -1,0 +1,116 @@
+"""Tensor-level calls into the CUDA library (device tensors in, device tensors out).
+
+Wavefunction tensors are (nk, nb, n_tot) complex, contiguous, on the sphere's
+device; every call is asynchronous on the current torch stream and raises
+``QgbError`` on a nonzero status.  There is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import torch
+
+from . import _lib
+from .sphere import DeviceSphere
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _qdtype(t: torch.Tensor) -> int:
+    if t.dtype == torch.complex128:
+        return _lib.QGB_F64
+    if t.dtype == torch.complex64:
+        return _lib.QGB_F32
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def _check_wf(sphere: DeviceSphere, C: torch.Tensor, name: str = "C") -> int:
+    if not C.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor (no CPU path)")
+    if C.dtype != sphere.cdtype:
+        raise TypeError(f"{name} dtype {C.dtype} != sphere dtype {sphere.cdtype}")
+    if C.dim() != 3 or C.shape[0] != sphere.tables.nk or C.shape[2] != sphere.tables.n_tot:
+        raise ValueError(f"{name} shape {tuple(C.shape)} != (nk={sphere.tables.nk}, nb, n_tot={sphere.tables.n_tot})")
+    if not C.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    return C.shape[1]
+
+
+def workspace(nbytes: int, device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+
+
+def apply_ke(sphere: DeviceSphere, C: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    nb = _check_wf(sphere, C)
+    out = torch.empty_like(C) if out is None else out
+    _check_wf(sphere, out, "out")
+    _lib.check(_lib.lib().qgb_apply_ke(ct.byref(sphere.struct), sphere.qdtype, C.data_ptr(), out.data_ptr(),
+                                       nb, _stream()), "apply_ke")
+    return out
+
+
+def apply_potential(sphere: DeviceSphere, C: torch.Tensor, out: torch.Tensor | None = None,
+                    add_ke: bool = False, accumulate: bool = False,
+                    ws: torch.Tensor | None = None) -> torch.Tensor:
+    """V*C (+ KE*C) on the G-sphere; `out` may alias `C`."""
+    if sphere.struct.V == 0:
+        raise RuntimeError("no potential installed (DeviceSphere.set_potential)")
+    nb = _check_wf(sphere, C)
+    out = torch.empty_like(C) if out is None else out
+    _check_wf(sphere, out, "out")
+    if ws is None:
+        ws = workspace(sphere.workspace_bytes(nb), C.device)
+    flags = (_lib.QGB_ADD_KE if add_ke else 0) | (_lib.QGB_ACCUMULATE if accumulate else 0)
+    _lib.check(_lib.lib().qgb_apply_potential(ct.byref(sphere.struct), sphere.qdtype, C.data_ptr(),
+                                              out.data_ptr(), nb, flags, ws.data_ptr(), ws.numel(),
+                                              _stream()), "apply_potential")
+    return out
+
+
+def project(beta: torch.Tensor, C: torch.Tensor, projT: torch.Tensor | None = None) -> torch.Tensor:
+    """projT[k, b, p] = <beta_p|C_b> (band-major projections)."""
+    nk, P, n_tot = beta.shape
+    nb = C.shape[1]
+    if C.dtype != beta.dtype or C.shape[0] != nk or C.shape[2] != n_tot:
+        raise ValueError("beta / C mismatch")
+    projT = torch.empty((nk, nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
+    _lib.check(_lib.lib().qgb_project(_qdtype(C), beta.data_ptr(), C.data_ptr(), projT.data_ptr(), nk, P, nb,
+                                      n_tot, _stream()), "project")
+    return projT
+
+
+def apply_nonlocal(beta: torch.Tensor, D_blocks: torch.Tensor, projT: torch.Tensor, out: torch.Tensor,
+                   work: torch.Tensor | None = None) -> torch.Tensor:
+    """out += beta D <beta|C> with D given as (n_atoms, pa, pa) blocks."""
+    nk, P, n_tot = beta.shape
+    n_atoms, pa, _ = D_blocks.shape
+    nb = projT.shape[1]
+    if n_atoms * pa != P:
+        raise ValueError("D blocks do not cover the projectors")
+    work = torch.empty_like(projT) if work is None else work
+    _lib.check(_lib.lib().qgb_apply_nonlocal(_qdtype(out), beta.data_ptr(), D_blocks.data_ptr(), n_atoms, pa,
+                                             projT.data_ptr(), out.data_ptr(), nk, nb, n_tot, work.data_ptr(),
+                                             _stream()), "apply_nonlocal")
+    return out
+
+
+def hamiltonian(sphere: DeviceSphere, C: torch.Tensor, beta: torch.Tensor | None, D_blocks: torch.Tensor | None,
+                out: torch.Tensor | None = None, projT: torch.Tensor | None = None):
+    """(HC, projT): HC = KE C + V C + beta D <beta|C> in one C-ABI call."""
+    nb = _check_wf(sphere, C)
+    out = torch.empty_like(C) if out is None else out
+    if beta is None or beta.shape[1] == 0:
+        n_atoms, pa, P = 0, 0, 0
+        bptr = dptr = pptr = 0
+    else:
+        n_atoms, pa, _ = D_blocks.shape
+        P = beta.shape[1]
+        projT = torch.empty((C.shape[0], nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
+        bptr, dptr, pptr = beta.data_ptr(), D_blocks.data_ptr(), projT.data_ptr()
+    ws = workspace(sphere.hamiltonian_workspace_bytes(nb, P), C.device)
+    _lib.check(_lib.lib().qgb_hamiltonian(ct.byref(sphere.struct), sphere.qdtype, C.data_ptr(), out.data_ptr(),
+                                          nb, bptr, dptr, n_atoms, pa, pptr, ws.data_ptr(), ws.numel(),
+                                          _stream()), "hamiltonian")
+    return out, projT

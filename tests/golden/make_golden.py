@@ -1,0 +1,195 @@
+"""Generate golden fixtures by running the reference package (nohm-devices/qimpy).
+
+Run in a container where the reference source is available:
+
+    python tests/golden/make_golden.py [--ref /root/reference/src] [--only NAME ...]
+
+The reference is imported unmodified.  Its missing optional dependencies
+(mpi4py, h5py, yaml, svg.path) are replaced by the single-rank stand-ins in
+``tests/golden/_shims``, and its pybind11 ``BufferView`` by a pass-through.
+Inputs come from ``qimpy_gb300.workloads`` (seeded, platform independent): the
+same lattice, k-mesh, cutoff and grid build the reference ``System``; the
+synthetic V(r), projectors beta and D matrix are injected into it the way the
+reference's fixed-Hamiltonian path holds them (``electrons.n_tilde.grad``,
+``ions.beta``, ``ions.D_all``, ``ions.beta_version``).
+
+Outputs, one ``.npz`` per workload in ``tests/golden/``:
+
+* ``n``, ``fft_index``: the reference's basis layout (qimpy/dft/electrons/_basis.py:167-204);
+* ``ke_pot_nl`` checks: H.psi of the seeded start vectors through
+  ``Electrons.hamiltonian`` (qimpy/dft/electrons/_hamiltonian.py:7-29), stored in
+  full for small cases and as per-band checksums plus a few full bands otherwise;
+* ``proj``: <beta|psi> (qimpy/dft/electrons/_wavefunction.py:106-123) for the same bands;
+* ``eig``: converged Davidson eigenvalues (qimpy/dft/electrons/_davidson.py:141-235)
+  from the Cholesky-orthonormalised start vectors, with the iteration count.
+
+Nothing here runs at test time; tests read the ``.npz`` files only.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import time
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from qimpy_gb300 import workloads as wl  # noqa: E402
+from qimpy_gb300.checksums import band_checksums  # noqa: E402
+
+#: workload -> (bands whose full H.psi is stored, Davidson settings or None)
+CASES = {
+    "tiny_fcc": dict(full=True, davidson=dict(n_iterations=200, eig_threshold=1e-12)),
+    "tiny_ortho": dict(full=True, davidson=dict(n_iterations=200, eig_threshold=1e-12)),
+    "si2": dict(full=False, sample=((0, 0), (0, 5), (3, 17), (7, 9)), n_hpsi_bands=18,
+                davidson=dict(n_iterations=300, eig_threshold=1e-11)),
+    "si64": dict(full=False, sample=((0, 0), (0, 7)), n_hpsi_bands=8,
+                 davidson=dict(n_iterations=300, eig_threshold=1e-9)),
+    "cu32": dict(full=False, sample=((0, 0), (3, 3)), n_hpsi_bands=4,
+                 davidson=dict(n_iterations=300, eig_threshold=1e-9)),
+}
+
+
+def import_reference(ref_src: str):
+    sys.path[:0] = [os.path.join(HERE, "_shims"), ref_src]
+    bv = types.ModuleType("qimpy.mpi._bufferview")
+    bv.BufferView = lambda t: t
+    sys.modules["qimpy.mpi._bufferview"] = bv
+    import qimpy  # noqa: F401
+    import torch
+
+    qimpy.rc.init(cores_override=os.cpu_count())
+    torch.set_num_threads(os.cpu_count())
+    return qimpy
+
+
+def build_system(qimpy, prob: wl.Problem, davidson: dict | None):
+    from qimpy.dft import System
+
+    size, offset = prob.kmesh
+    el_cfg = {
+        "k-mesh": {"size": list(size), "offset": list(offset), "use-inversion": False},
+        "basis": {"ke-cutoff": prob.ke_cutoff, "grid": {"shape": list(prob.grid_shape)}},
+        "fillings": {"n-bands": prob.n_bands, "n-bands-extra": prob.n_bands_extra},
+        "lcao": False,
+    }
+    if davidson:
+        el_cfg["davidson"] = {k.replace("_", "-"): v for k, v in davidson.items()}
+    R = prob.Rbasis
+    return System(
+        lattice=dict(vector1=list(R[:, 0]), vector2=list(R[:, 1]), vector3=list(R[:, 2])),
+        symmetries={"override": "identity"},
+        grid={"shape": list(prob.grid_shape)},
+        electrons=el_cfg,
+        process_grid_shape=(1, 1, 1),
+    )
+
+
+def inject(qimpy, system, prob, beta_np):
+    """Install V(r), beta and D into the reference objects."""
+    import torch
+    from qimpy.grid import FieldR
+    from qimpy.dft.electrons import Wavefunction
+
+    el = system.electrons
+    basis = el.basis
+    shape = tuple(prob.grid_shape)
+    el.n_tilde = ~FieldR(basis.grid, data=torch.zeros((1,) + shape, dtype=torch.float64))
+    el.n_tilde.grad = ~FieldR(basis.grid, data=torch.from_numpy(prob.V_r)[None].clone())
+    ions = system.ions
+    beta = torch.from_numpy(beta_np)[None, :, :, None, :].clone()
+    ions.beta = Wavefunction(basis, coeff=beta)
+    ions.D_all = torch.from_numpy(prob.D_all()).to(torch.complex128)
+    ions.beta_version += 1
+    # Zero wavefunctions size their cached projections by ions.n_projectors,
+    # a property derived from pseudopotential files; report the injected count.
+    ions.__class__ = type("InjectedIons", (type(ions),), {"n_projectors": prob.n_projectors})
+    return el
+
+
+def run_case(qimpy, name: str, cfg: dict, out_dir: str) -> None:
+    import torch
+    from qimpy.dft.electrons import Wavefunction
+
+    t0 = time.time()
+    prob = wl.get(name)
+    mine = wl.make_basis(prob.Gbasis, prob.k, prob.ke_cutoff, prob.grid_shape)
+    system = build_system(qimpy, prob, cfg.get("davidson"))
+    el = system.electrons
+    basis = el.basis
+    ref_n = basis.n.numpy().astype(np.int64)
+    ref_index = basis.fft_index.numpy().astype(np.int64)
+    assert np.array_equal(ref_n, mine.n), (ref_n, mine.n)
+    assert np.array_equal(ref_index, mine.fft_index)
+    beta = wl.make_projectors(prob, mine)
+    el = inject(qimpy, system, prob, beta)
+    n_bands_tot = prob.n_bands + prob.n_bands_extra
+    C0 = wl.make_wavefunctions(prob, mine, n_bands_tot)
+    out: dict = dict(
+        n=ref_n,
+        fft_index=ref_index.astype(np.int32),
+        ke_ref=basis.get_ke().numpy()[:, :8].copy(),
+        Gbasis_ref=system.lattice.Gbasis.numpy(),
+        k_ref=basis.k.numpy(),
+    )
+
+    # --- H.psi of the (not orthonormalised) start vectors:
+    nb = n_bands_tot if cfg["full"] else cfg["n_hpsi_bands"]
+    C = Wavefunction(basis, coeff=torch.from_numpy(C0[None, :, :nb, None, :]).clone())
+    t1 = time.time()
+    HC = el.hamiltonian(C).coeff[0, :, :, 0, :].numpy()
+    t_hpsi = time.time() - t1
+    proj = C.proj[0].numpy()  # (nk, P, nb)
+    out["hpsi_bands"] = np.int64(nb)
+    out["hpsi_seconds"] = np.float64(t_hpsi)
+    if cfg["full"]:
+        out["hpsi"] = HC
+        out["proj"] = proj
+        out["C0"] = C0
+        out["V_r"] = prob.V_r
+        out["beta"] = beta
+    else:
+        sample = cfg["sample"]
+        out["hpsi_sample_kb"] = np.array(sample, dtype=np.int64)
+        out["hpsi_sample"] = np.stack([HC[k, b] for k, b in sample])
+        out["proj_sample"] = np.stack([proj[k, :, b] for k, b in sample])
+    out["hpsi_checksums"] = band_checksums(HC, ref_n)
+
+    # --- Davidson:
+    dav = cfg.get("davidson")
+    if dav:
+        el.C = Wavefunction(basis, coeff=torch.from_numpy(C0[None, :, :, None, :]).clone())
+        el.C = el.C.orthonormalize()
+        t1 = time.time()
+        el.diagonalize()
+        out["davidson_seconds"] = np.float64(time.time() - t1)
+        out["eig"] = el.eig[0].numpy().copy()
+        out["davidson_iterations"] = np.int64(el.diagonalize._i_iter)
+        out["eig_threshold"] = np.float64(dav["eig_threshold"])
+    path = os.path.join(out_dir, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: wrote {path} ({os.path.getsize(path) / 1e3:.0f} KB) in {time.time() - t0:.1f} s"
+          f"; H.psi {t_hpsi * 1e3:.1f} ms for {nb} bands"
+          + (f"; Davidson {out['davidson_iterations']} it, {out['davidson_seconds']:.1f} s" if dav else ""))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference/src")
+    ap.add_argument("--only", nargs="*", default=None)
+    ap.add_argument("--out", default=HERE)
+    args = ap.parse_args()
+    qimpy = import_reference(args.ref)
+    for name, cfg in CASES.items():
+        if args.only and name not in args.only:
+            continue
+        run_case(qimpy, name, cfg, args.out)
+
+
+if __name__ == "__main__":
+    main()
