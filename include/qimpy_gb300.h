@@ -155,7 +155,7 @@ size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int d
 
 /*
  * Diagnostic: `blocks` x `threads` threads each run 8 independent FMA chains
- * for 8*iters steps (16*iters flops per thread) in the given dtype.  Timed by
+ * of 8*iters steps (64*iters FMAs = 128*iters flops per thread).  Timed by
  * the caller; gives the FP64/FP32 CUDA-core peak used as a roofline
  * denominator.  `out` receives nothing in practice (needs `blocks` reals).
  * No reference counterpart (measurement aid).

@@ -10,7 +10,8 @@ import os
 import threading
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libqimpy_gb300.so")
+DEBUG = os.environ.get("QGB_DEBUG_CHECKS", "0") == "1"
+LIB_PATH = os.path.join(PKG, "libqimpy_gb300_debug.so" if DEBUG else "libqimpy_gb300.so")
 
 QGB_F64, QGB_F32 = 0, 1
 QGB_ADD_KE, QGB_ACCUMULATE = 1, 2
@@ -79,10 +80,21 @@ def lib() -> ct.CDLL:
                     fn = getattr(handle, name)
                     fn.restype = res
                     fn.argtypes = args
+                if DEBUG:
+                    handle.qgb_debug_violation.restype = ct.c_int
+                    handle.qgb_debug_violation.argtypes = [ct.POINTER(ct.c_ulonglong)]
                 if handle.qgb_abi_version() != ABI_VERSION:
                     raise RuntimeError("libqimpy_gb300.so ABI version mismatch; rebuild it")
                 _lib = handle
     return _lib
+
+
+def debug_violation() -> tuple:
+    """(site, index, limit, block) of the first range violation since the last
+    call (debug library only); site 0 means none."""
+    out = (ct.c_ulonglong * 4)()
+    check(lib().qgb_debug_violation(out), "debug_violation")
+    return tuple(int(x) for x in out)
 
 
 def check(status: int, what: str) -> None:

@@ -16,6 +16,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libqimpy_gb300.so")
+#: Range-checked variant (-DQGB_DEBUG_CHECKS), loaded when QGB_DEBUG_CHECKS=1.
+DEBUG_LIB = os.path.join(PKG, "libqimpy_gb300_debug.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -51,8 +53,8 @@ def headers() -> list[str]:
     return hs + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
 
 
-def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+def _compile(src: str, extra: list[str], build_dir: str = BUILD) -> str:
+    obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
     newest_dep = max([_mtime(src)] + [_mtime(h) for h in headers()])
     if _mtime(obj) >= newest_dep:
         return obj
@@ -63,27 +65,30 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
-    """Compile and link the library; returns its path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, debug: bool = False) -> str:
+    """Compile and link the library (or its range-checked debug variant); returns its path."""
+    build_dir = BUILD + ("_debug" if debug else "")
+    lib = DEBUG_LIB if debug else LIB
+    extra = ["-DQGB_DEBUG_CHECKS"] if debug else []
+    os.makedirs(build_dir, exist_ok=True)
     _regen_codelets()
     if force:
-        for f in os.listdir(BUILD):
+        for f in os.listdir(build_dir):
             if f.endswith(".o"):
-                os.remove(os.path.join(BUILD, f))
+                os.remove(os.path.join(build_dir, f))
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra_flags or []), srcs))
-    if force or _mtime(LIB) < max(_mtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcublas"]
+        objs = list(ex.map(lambda s: _compile(s, extra, build_dir), srcs))
+    if force or _mtime(lib) < max(_mtime(o) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs + ["-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(LIB + ".tmp", LIB)
+        os.replace(lib + ".tmp", lib)
         if verbose:
-            print(f"built {LIB}")
-    return LIB
+            print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build(force="--force" in sys.argv, verbose=True, debug="--debug" in sys.argv)

@@ -37,6 +37,9 @@ int project(int dtype, const void* beta, const void* C, void* projT, int nk, int
             cudaStream_t st);
 int apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int pa, const void* projT,
                    void* out, int nk, int nb, int n_tot, void* work, cudaStream_t st);
+#ifdef QGB_DEBUG_CHECKS
+int debug_violation(unsigned long long* out4);
+#endif
 
 }  // namespace qgb
 
@@ -118,5 +121,9 @@ int qgb_hamiltonian(const qgb_sphere* s, int dtype, const void* C, void* HC, int
   }
   return QGB_OK;
 }
+
+#ifdef QGB_DEBUG_CHECKS
+int qgb_debug_violation(unsigned long long* out4) { return qgb::debug_violation(out4); }
+#endif
 
 }  // extern "C"

@@ -15,6 +15,10 @@
 // with W[i][j] = exp(+2 pi i i j / L).  Real-space index r = a + L2 b lives at
 // position L1 a + b ("digit-permuted" order); every pass reads and writes the
 // same addresses from one thread, so a pass needs no barrier inside it.
+//
+// All data and twiddles live in the kernel's dynamic shared memory and are
+// addressed by element offsets from its base, so every access is a plain
+// shared-memory load or store.
 #pragma once
 
 #include "codelets.cuh"
@@ -22,24 +26,33 @@
 
 namespace qgb {
 
-// One codelet applied in place to p[j * stride], j < R, with an optional
-// twiddle multiply tw[j * tw_stride] on the outputs (table holds exp(+i...),
-// conjugated when SIGN < 0).
+extern __shared__ __align__(16) unsigned char qgb_smem[];
+
+template <typename T> __device__ __forceinline__ cplx_t<T>* smem_c() {
+  return reinterpret_cast<cplx_t<T>*>(qgb_smem);
+}
+
+// One codelet applied in place to smem[off + j * stride], j < R, with an
+// optional twiddle multiply by smem[tw + j * tw_stride] (tw < 0: none) on the
+// outputs; the table holds exp(+i...), conjugated when SIGN < 0.
 template <typename T, int S, int R>
-__device__ __forceinline__ void codelet_inplace(cplx_t<T>* __restrict__ p, int stride,
-                                                const cplx_t<T>* __restrict__ tw, int tw_stride) {
+__device__ __forceinline__ void codelet_inplace(int off, int stride, int tw, int tw_stride, int lim,
+                                                int tw_lim) {
+  cplx_t<T>* sm = smem_c<T>();
   T re[R], im[R];
 #pragma unroll
   for (int j = 0; j < R; ++j) {
-    const cplx_t<T> v = p[j * stride];
+    if (!QGB_OK_IDX(off + j * stride, lim, 10 + R)) return;
+    const cplx_t<T> v = sm[off + j * stride];
     re[j] = v.x;
     im[j] = v.y;
   }
   Codelet<R, S>::run(re, im);
-  if (tw != nullptr) {
+  if (tw >= 0) {
 #pragma unroll
     for (int j = 1; j < R; ++j) {
-      const cplx_t<T> w = tw[j * tw_stride];
+      if (!QGB_OK_IDX(tw + j * tw_stride, tw_lim, 40 + R)) return;
+      const cplx_t<T> w = sm[tw + j * tw_stride];
       const T wy = (S > 0) ? w.y : -w.y;
       const T xr = re[j] * w.x - im[j] * wy;
       const T xi = re[j] * wy + im[j] * w.x;
@@ -48,35 +61,34 @@ __device__ __forceinline__ void codelet_inplace(cplx_t<T>* __restrict__ p, int s
     }
   }
 #pragma unroll
-  for (int j = 0; j < R; ++j) p[j * stride] = mk<T>(re[j], im[j]);
+  for (int j = 0; j < R; ++j) sm[off + j * stride] = mk<T>(re[j], im[j]);
 }
 
 // Geometry of one pass: item `it` in [0, nbatch * nsub) is (batch = it % nbatch,
-// sub = it / nbatch); its codelet elements sit at
+// sub = it / nbatch); its codelet elements sit at shared offsets
 //   base + boff(batch) + sub * sstride + j * estride,
-// boff(batch) = (bmap ? bmap[batch] : batch) * bstride.
-template <typename T> struct Pass {
-  cplx_t<T>* base;
+// boff(batch) = (bmap ? bmap[batch] : batch) * bstride, bmap in global memory.
+struct Pass {
   const int* bmap;
-  int nbatch, bstride, nsub, sstride, estride;
-  const cplx_t<T>* tw;  // nullptr: no twiddles
-  int tw_sub, tw_el;
+  int base, nbatch, bstride, nsub, sstride, estride;
+  int tw, tw_sub, tw_el;  // tw < 0: no twiddles
+  int lim, tw_lim;        // bounds of the data and twiddle regions (debug checks)
 };
 
 template <typename T, int S, int R>
-__device__ __noinline__ void run_pass_R(const Pass<T> ps) {
+__device__ __forceinline__ void run_pass_R(const Pass ps) {
   const int nitems = ps.nbatch * ps.nsub;
   for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
     const int sub = it / ps.nbatch;
     const int b = it - sub * ps.nbatch;
-    const int boff = (ps.bmap ? ps.bmap[b] : b) * ps.bstride;
+    const int boff = (ps.bmap != nullptr ? __ldg(ps.bmap + b) : b) * ps.bstride;
     codelet_inplace<T, S, R>(ps.base + boff + sub * ps.sstride, ps.estride,
-                             ps.tw ? ps.tw + sub * ps.tw_sub : nullptr, ps.tw_el);
+                             ps.tw >= 0 ? ps.tw + sub * ps.tw_sub : -1, ps.tw_el, ps.lim, ps.tw_lim);
   }
 }
 
 template <typename T, int S>
-__device__ void run_pass(int R, const Pass<T>& ps) {
+__device__ __forceinline__ void run_pass(int R, const Pass ps) {
   switch (R) {
     case 2: run_pass_R<T, S, 2>(ps); break;
     case 3: run_pass_R<T, S, 3>(ps); break;
@@ -95,32 +107,33 @@ __device__ void run_pass(int R, const Pass<T>& ps) {
   }
 }
 
-// Inverse transform (natural -> permuted) of nbatch pencils, element stride es.
-// Ends with __syncthreads().
+// Inverse transform (natural -> permuted) of nbatch pencils starting at shared
+// offset `base`, element stride es; twiddles at shared offset W; `lim` bounds
+// the data region.  Ends with __syncthreads().
 template <typename T>
-__device__ void fft_inverse(cplx_t<T>* base, const int* bmap, int nbatch, int bstride, int es,
-                            int L1, int L2, const cplx_t<T>* W) {
+__device__ __forceinline__ void fft_inverse(int base, const int* bmap, int nbatch, int bstride, int es,
+                                            int L1, int L2, int W, int lim) {
   if (L2 > 1) {
-    run_pass<T, +1>(L2, Pass<T>{base, bmap, nbatch, bstride, L1, es, L1 * es, W, L2, 1});
+    run_pass<T, +1>(L2, Pass{bmap, base, nbatch, bstride, L1, es, L1 * es, W, L2, 1, lim, W + L1 * L2});
     __syncthreads();
   }
   if (L1 > 1) {
-    run_pass<T, +1>(L1, Pass<T>{base, bmap, nbatch, bstride, L2, L1 * es, es, nullptr, 0, 0});
+    run_pass<T, +1>(L1, Pass{bmap, base, nbatch, bstride, L2, L1 * es, es, -1, 0, 0, lim, 0});
     __syncthreads();
   }
 }
 
 // Forward transform (permuted -> natural) of nbatch pencils.  Ends with __syncthreads().
 template <typename T>
-__device__ void fft_forward(cplx_t<T>* base, const int* bmap, int nbatch, int bstride, int es,
-                            int L1, int L2, const cplx_t<T>* W) {
+__device__ __forceinline__ void fft_forward(int base, const int* bmap, int nbatch, int bstride, int es,
+                                            int L1, int L2, int W, int lim) {
   if (L1 > 1) {
-    run_pass<T, -1>(L1, Pass<T>{base, bmap, nbatch, bstride, L2, L1 * es, es,
-                                (L2 > 1) ? W : nullptr, 1, L2});
+    run_pass<T, -1>(L1, Pass{bmap, base, nbatch, bstride, L2, L1 * es, es, (L2 > 1) ? W : -1, 1, L2, lim,
+                             W + L1 * L2});
     __syncthreads();
   }
   if (L2 > 1) {
-    run_pass<T, -1>(L2, Pass<T>{base, bmap, nbatch, bstride, L1, es, L1 * es, nullptr, 0, 0});
+    run_pass<T, -1>(L2, Pass{bmap, base, nbatch, bstride, L1, es, L1 * es, -1, 0, 0, lim, 0});
     __syncthreads();
   }
 }

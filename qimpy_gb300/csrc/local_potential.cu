@@ -38,8 +38,9 @@ struct LocalParams {
 };
 
 template <typename T>
-__device__ __forceinline__ void load_twiddles(cplx_t<T>* dst, const cplx_t<T>* src, int count) {
-  for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = src[i];
+__device__ __forceinline__ void load_twiddles(int dst, const cplx_t<T>* src, int count) {
+  cplx_t<T>* sm = smem_c<T>();
+  for (int i = threadIdx.x; i < count; i += blockDim.x) sm[dst + i] = src[i];
 }
 
 // Plane workspace index of (k, band-in-chunk, slab).
@@ -55,17 +56,15 @@ __global__ void __launch_bounds__(kThreads) k_ifft_yz(const qgb_sphere s, LocalP
   const int slab = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
   if (slab >= s.n_slabs[k]) return;
   const int N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  C2* P = reinterpret_cast<C2*>(smem_raw);
-  C2* Wy = P + N1 * ld;
-  C2* Wz = Wy + N1;
+  const int lim = N1 * ld, Wy = lim, Wz = Wy + N1;  // shared layout: plane, W_y, W_z
+  C2* sm = smem_c<T>();
   const C2* tw = static_cast<const C2*>(s.twiddle);
   load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
   load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
   const C2 zero = mk<T>(T(0), T(0));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int r = warp; r < N1; r += nwarps)
-    for (int c = lane; c < N2; c += 32) P[r * ld + c] = zero;
+    for (int c = lane; c < N2; c += 32) sm[r * ld + c] = zero;
   __syncthreads();
 
   // Scatter this slab's coefficients (contiguous in the basis) into the plane.
@@ -74,21 +73,25 @@ __global__ void __launch_bounds__(kThreads) k_ifft_yz(const qgb_sphere s, LocalP
   const C2* Cb = C + (static_cast<size_t>(k) * lp.nb_total + lp.b0 + b) * s.n_tot;
   const int* yz = s.yz + static_cast<size_t>(k) * s.n_tot;
   for (int g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
+    if (!QGB_OK_IDX(g, s.n[k], 1)) continue;
     const int v = yz[g];
-    P[(v >> 16) * ld + (v & 0xFFFF)] = Cb[g];
+    const int pos = (v >> 16) * ld + (v & 0xFFFF);
+    if (!QGB_OK_IDX(pos, lim, 2) || !QGB_OK_IDX(v & 0xFFFF, N2, 3)) continue;
+    sm[pos] = Cb[g];
   }
   __syncthreads();
 
   // Inverse z-FFT along the rows this slab touches (row stride ld, element stride 1).
   const int r0 = s.row_start[k * (s.max_slabs + 1) + slab];
   const int nrows = s.row_start[k * (s.max_slabs + 1) + slab + 1] - r0;
-  fft_inverse<T>(P, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz);
+  fft_inverse<T>(0, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz, lim);
   // Inverse y-FFT along all N2 columns (column stride 1, element stride ld).
-  fft_inverse<T>(P, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy);
+  fft_inverse<T>(0, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy, lim);
 
+  if (!QGB_OK_IDX(plane_index(s, k, b, lp.nb, slab), (long long)s.nk * lp.nb * s.max_slabs, 4)) return;
   C2* out = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
   for (int r = warp; r < N1; r += nwarps)
-    for (int c = lane; c < N2; c += 32) out[r * N2 + c] = P[r * ld + c];
+    for (int c = lane; c < N2; c += 32) out[r * N2 + c] = sm[r * ld + c];
 }
 
 template <typename T>
@@ -98,15 +101,14 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
   const int r1 = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
   const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
   const int L1 = s.L1[0], L2 = s.L2[0];
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  C2* X = reinterpret_cast<C2*>(smem_raw);
-  C2* Wx = X + N0 * ld;
+  const int lim = N0 * ld, Wx = lim;  // shared layout: pencils (x rows of N2 columns), W_x
+  C2* sm = smem_c<T>();
   const C2* tw = static_cast<const C2*>(s.twiddle);
   load_twiddles<T>(Wx, tw + s.tw_off[0], N0);
   const C2 zero = mk<T>(T(0), T(0));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int r = warp; r < N0; r += nwarps)
-    for (int c = lane; c < N2; c += 32) X[r * ld + c] = zero;
+    for (int c = lane; c < N2; c += 32) sm[r * ld + c] = zero;
   __syncthreads();
 
   const int nslabs = s.n_slabs[k];
@@ -114,15 +116,18 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
   const size_t plane = static_cast<size_t>(N1) * N2;
   C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2;
   for (int sl = warp; sl < nslabs; sl += nwarps) {
+    const int x = i0[sl];
+    if (!QGB_OK_IDX(x, N0, 5) ||
+        !QGB_OK_IDX(plane_index(s, k, b, lp.nb, sl), (long long)s.nk * lp.nb * s.max_slabs, 6))
+      continue;
     const C2* src = base + sl * plane;
-    C2* dst = X + i0[sl] * ld;
-    for (int c = lane; c < N2; c += 32) dst[c] = src[c];
+    for (int c = lane; c < N2; c += 32) sm[x * ld + c] = src[c];
   }
   __syncthreads();
 
   // Inverse x pass 1 (natural in).
   if (L2 > 1) {
-    run_pass<T, +1>(L2, Pass<T>{X, nullptr, N2, 1, L1, ld, L1 * ld, Wx, L2, 1});
+    run_pass<T, +1>(L2, Pass{nullptr, 0, N2, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
     __syncthreads();
   }
   // Inverse pass 2, multiply by V at the permuted real-space position, forward
@@ -133,15 +138,19 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
     for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
       const int a = it / N2;
       const int c = it - a * N2;
-      C2* p = X + c + a * L1 * ld;
+      const int p = c + a * L1 * ld;
       const T* Vp = V + (static_cast<size_t>(a) * L1 * N1 + r1) * N2 + c;
+      if (!QGB_OK_IDX(c + (a * L1 + L1 - 1) * ld, lim, 7) ||
+          !QGB_OK_IDX(((long long)(a * L1 + L1 - 1) * N1 + r1) * N2 + c, (long long)N0 * N1 * N2, 8) ||
+          !QGB_OK_IDX((L1 - 1) * L2 + a, N0, 9))
+        continue;
       // L1 is a codelet size; dispatch once per item.
       switch (L1) {
 #define QGB_XMID(R)                                                                        \
   case R: {                                                                                \
     T re[R], im[R];                                                                        \
     _Pragma("unroll") for (int j = 0; j < R; ++j) {                                        \
-      const C2 v = p[j * ld];                                                              \
+      const C2 v = sm[p + j * ld];                                                         \
       re[j] = v.x;                                                                         \
       im[j] = v.y;                                                                         \
     }                                                                                      \
@@ -154,14 +163,14 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
     Codelet<R, -1>::run(re, im);                                                           \
     if (L2 > 1) {                                                                          \
       _Pragma("unroll") for (int j = 1; j < R; ++j) {                                      \
-        const C2 w = Wx[j * L2 + a];                                                       \
+        const C2 w = sm[Wx + j * L2 + a];                                                  \
         const T xr = re[j] * w.x + im[j] * w.y;                                            \
         const T xi = im[j] * w.x - re[j] * w.y;                                            \
         re[j] = xr;                                                                        \
         im[j] = xi;                                                                        \
       }                                                                                    \
     }                                                                                      \
-    _Pragma("unroll") for (int j = 0; j < R; ++j) p[j * ld] = mk<T>(re[j], im[j]);         \
+    _Pragma("unroll") for (int j = 0; j < R; ++j) sm[p + j * ld] = mk<T>(re[j], im[j]);    \
   } break;
         QGB_XMID(1)
         QGB_XMID(2)
@@ -185,20 +194,21 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
   }
   // Forward pass B (natural out).
   if (L2 > 1) {
-    run_pass<T, -1>(L2, Pass<T>{X, nullptr, N2, 1, L1, ld, L1 * ld, nullptr, 0, 0});
+    run_pass<T, -1>(L2, Pass{nullptr, 0, N2, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
     __syncthreads();
   }
   for (int sl = warp; sl < nslabs; sl += nwarps) {
+    const int x = i0[sl];
+    if (!QGB_OK_IDX(x, N0, 5)) continue;
     C2* dst = base + sl * plane;
-    const C2* src = X + i0[sl] * ld;
-    for (int c = lane; c < N2; c += 32) dst[c] = src[c];
+    for (int c = lane; c < N2; c += 32) dst[c] = sm[x * ld + c];
   }
 }
 
+// C and out may alias (in-place apply): no __restrict__ on them.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, LocalParams lp,
-                                                            const cplx_t<T>* __restrict__ C,
-                                                            cplx_t<T>* __restrict__ out,
+                                                            const cplx_t<T>* C, cplx_t<T>* out,
                                                             const cplx_t<T>* __restrict__ planes) {
   using C2 = cplx_t<T>;
   const int slab = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
@@ -211,23 +221,22 @@ __global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, 
   }
   if (slab >= nslabs) return;
   const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  C2* P = reinterpret_cast<C2*>(smem_raw);
-  C2* Wy = P + N1 * ld;
-  C2* Wz = Wy + N1;
+  const int lim = N1 * ld, Wy = lim, Wz = Wy + N1;
+  C2* sm = smem_c<T>();
   const C2* tw = static_cast<const C2*>(s.twiddle);
   load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
   load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  if (!QGB_OK_IDX(plane_index(s, k, b, lp.nb, slab), (long long)s.nk * lp.nb * s.max_slabs, 4)) return;
   const C2* in = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
   for (int r = warp; r < N1; r += nwarps)
-    for (int c = lane; c < N2; c += 32) P[r * ld + c] = in[r * N2 + c];
+    for (int c = lane; c < N2; c += 32) sm[r * ld + c] = in[r * N2 + c];
   __syncthreads();
 
-  fft_forward<T>(P, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy);
+  fft_forward<T>(0, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy, lim);
   const int r0 = s.row_start[k * (s.max_slabs + 1) + slab];
   const int nrows = s.row_start[k * (s.max_slabs + 1) + slab + 1] - r0;
-  fft_forward<T>(P, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz);
+  fft_forward<T>(0, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz, lim);
 
   const int g0 = s.slab_start[k * (s.max_slabs + 1) + slab];
   const int g1 = s.slab_start[k * (s.max_slabs + 1) + slab + 1];
@@ -237,8 +246,11 @@ __global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, 
   const bool add_ke = (lp.flags & QGB_ADD_KE) != 0;
   const T* ke = static_cast<const T*>(s.ke) + static_cast<size_t>(k) * s.n_tot;
   for (int g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
+    if (!QGB_OK_IDX(g, s.n[k], 1)) continue;
     const int v = yz[g];
-    const C2 f = P[(v >> 16) * ld + (v & 0xFFFF)];
+    const int pos = (v >> 16) * ld + (v & 0xFFFF);
+    if (!QGB_OK_IDX(pos, lim, 2)) continue;
+    const C2 f = sm[pos];
     T xr = f.x * invN, xi = f.y * invN;
     if (add_ke) {
       const C2 c = Cb[g];
@@ -273,6 +285,18 @@ __global__ void k_apply_ke(const qgb_sphere s, int nb, const cplx_t<T>* __restri
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
+
+#ifdef QGB_DEBUG_CHECKS
+// Debug builds: copy out and clear the first recorded range violation
+// (site, index, limit, packed block index); site 0 = none.
+int debug_violation(unsigned long long* out4) {
+  QGB_CUDA_CHECK(cudaDeviceSynchronize());
+  QGB_CUDA_CHECK(cudaMemcpyFromSymbol(out4, g_qgb_violation, 4 * sizeof(unsigned long long)));
+  const unsigned long long zero[4] = {0, 0, 0, 0};
+  QGB_CUDA_CHECK(cudaMemcpyToSymbol(g_qgb_violation, zero, sizeof(zero)));
+  return QGB_OK;
+}
+#endif
 
 static bool codelet_size(int R) {
   switch (R) {

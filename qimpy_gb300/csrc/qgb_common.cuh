@@ -23,6 +23,25 @@ template <typename T> __device__ __forceinline__ cplx_t<T> mk(T x, T y) {
   return r;
 }
 
+// Debug builds (-DQGB_DEBUG_CHECKS) range-check every shared and global access of
+// the local-potential kernels: a violation records (site, index, limit) in a device
+// word and the access is skipped, so a bad index is reported instead of faulting.
+#ifdef QGB_DEBUG_CHECKS
+static __device__ unsigned long long g_qgb_violation[4];
+__device__ __forceinline__ bool qgb_in_range(long long idx, long long lim, int site) {
+  if (idx >= 0 && idx < lim) return true;
+  if (atomicCAS(&g_qgb_violation[0], 0ull, (unsigned long long)site) == 0ull) {
+    g_qgb_violation[1] = (unsigned long long)idx;
+    g_qgb_violation[2] = (unsigned long long)lim;
+    g_qgb_violation[3] = ((unsigned long long)blockIdx.x << 32) | (blockIdx.y << 16) | blockIdx.z;
+  }
+  return false;
+}
+#define QGB_OK_IDX(idx, lim, site) ::qgb::qgb_in_range((long long)(idx), (long long)(lim), (site))
+#else
+#define QGB_OK_IDX(idx, lim, site) true
+#endif
+
 // Error state of the calling host thread.
 void set_error(const char* fmt, ...);
 int fail(int code, const char* fmt, ...);

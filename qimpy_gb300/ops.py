@@ -55,7 +55,7 @@ def apply_potential(sphere: DeviceSphere, C: torch.Tensor, out: torch.Tensor | N
                     add_ke: bool = False, accumulate: bool = False,
                     ws: torch.Tensor | None = None) -> torch.Tensor:
     """V*C (+ KE*C) on the G-sphere; `out` may alias `C`."""
-    if sphere.struct.V == 0:
+    if not sphere.struct.V:
         raise RuntimeError("no potential installed (DeviceSphere.set_potential)")
     nb = _check_wf(sphere, C)
     out = torch.empty_like(C) if out is None else out

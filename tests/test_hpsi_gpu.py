@@ -64,10 +64,13 @@ def test_hamiltonian_matches_reference_golden(name, dtype):
     assert _rel(projT.transpose(1, 2).cpu().numpy(), g["proj"]) < TOL[dtype]
 
 
-def test_si2_hamiltonian_checksums_fp64():
-    g = np.load(os.path.join(GOLDEN, "si2.npz"))
+@pytest.mark.parametrize("name", ["si2", "si64", "cu32"])
+def test_hamiltonian_checksums_fp64(name):
+    """Full-size H.psi against the reference's per-band checksums (1e-12 relative)."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
     nb = int(g["hpsi_bands"])
-    p, b, beta, C, ds = _setup("si2", torch.complex128, nbands=nb)
+    p, b, beta, C, ds = _setup(name, torch.complex128, nbands=nb)
+    assert np.array_equal(b.fft_index, g["fft_index"])
     Cd = torch.from_numpy(C).to(DEV)
     HC, _ = ops.hamiltonian(ds, Cd, torch.from_numpy(beta).to(DEV), torch.from_numpy(p.D_atom).to(DEV, torch.complex128))
     HC = HC.cpu().numpy()
