@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--cpu-sample-bands", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--eig-reps", type=int, default=3)
+    ap.add_argument("--no-eigensolve", action="store_true")
     return ap.parse_args()
 
 
@@ -306,6 +308,46 @@ def run_gb300(args, rank, ws, local):
     return p, b, tables, results, peaks
 
 
+def run_eigensolves(args, local):
+    """Davidson eigensolves/s on si2 (Si primitive cell, 8 k, 16 bands), FP64 and mixed.
+
+    One eigensolve = Davidson from the seeded start vectors to max |d eig| < 1e-10
+    (FP64) / 1e-6 (mixed, then one FP64 Rayleigh-Ritz refinement sweep), every
+    k-point, timed end to end with CUDA events (host syncs per iteration included).
+    Eigenvalue errors are against the reference's own FP64 eigenvalues."""
+    import torch
+
+    from qimpy_gb300 import davidson as dv, electrons as E, workloads as wl
+
+    dev = torch.device(f"cuda:{local}")
+    p = wl.get("si2")
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "si2.npz"))
+    el64, C0 = E.from_problem(p, dev, torch.complex128)
+    el32, _ = E.from_problem(p, dev, torch.complex64)
+    out = {}
+    for form, el, thr in (("fp64", el64, 1e-10), ("mixed", el32, 1e-6)):
+        times, stats = [], None
+        for rep in range(1 + max(1, args.eig_reps)):
+            el.C = E.Wavefunction(el.basis, coeff=C0.to(dev, el.basis.dtype)).orthonormalize()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            stats = dv.Davidson(el, n_iterations=300, eig_threshold=thr)()
+            eig = el.eig
+            if form == "mixed":
+                eig, _ = dv.refine_fp64(el, el64)
+            e1.record()
+            torch.cuda.synchronize()
+            if rep:  # first solve is warm-up
+                times.append(e0.elapsed_time(e1) * 1e-3)
+        err = float(np.abs(eig.cpu().numpy()[:, : p.n_bands] - gold["eig"][:, : p.n_bands]).max())
+        out[form] = dict(eigensolves_per_s=1.0 / float(np.median(times)), seconds=float(np.median(times)),
+                         p50_s=float(np.percentile(times, 50)), p99_s=float(np.percentile(times, 99)),
+                         iterations=stats.iterations, converged=stats.converged, hpsi_bands=stats.hpsi_bands,
+                         max_eig_error_ha_vs_reference=err)
+    return out
+
+
 def cpu_baseline(args, p=None, b=None, beta=None, C=None, threads=None):
     """Oracle H.psi (FP64, numpy/scipy) on a bounded band sample, timed on host cores."""
     from oracle import hpsi as oh
@@ -377,6 +419,8 @@ def main():
         "gpu_launches": mixed["launches_per_step"] * args.steps,
         "clocks": mixed["clocks"],
     }
+    if not args.no_eigensolve:
+        out["eigensolve_si2"] = run_eigensolves(args, local)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:

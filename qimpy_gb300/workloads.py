@@ -33,21 +33,26 @@ _M1 = np.uint64(0xBF58476D1CE4E5B9)
 _M2 = np.uint64(0x94D049BB133111EB)
 
 
-def splitmix_uniform(seed: int, stream: int, count: int) -> np.ndarray:
-    """`count` uniforms in (0, 1) from a counter-based splitmix64 stream.
+def splitmix_uniform_grid(seed: int, streams, counters) -> np.ndarray:
+    """Uniforms in (0, 1) for broadcastable arrays of stream ids and counters.
 
-    Element i is a pure function of (seed, stream, i): no state, no platform
-    dependence (integer arithmetic modulo 2^64, then the top 53 bits)."""
+    Element (stream, i) is a pure function of (seed, stream, i): no state, no
+    platform dependence (integer arithmetic modulo 2^64, then the top 53 bits)."""
+    streams = np.asarray(streams, dtype=np.uint64)
+    counters = np.asarray(counters, dtype=np.uint64)
     with np.errstate(over="ignore"):
-        base = (np.uint64(seed) * np.uint64(0x100000001B3)) ^ (
-            np.uint64(stream) * np.uint64(0xC2B2AE3D27D4EB4F)
-        )
-        x = base + (np.arange(1, count + 1, dtype=np.uint64) * _GOLD)
+        base = (np.uint64(seed) * np.uint64(0x100000001B3)) ^ (streams * np.uint64(0xC2B2AE3D27D4EB4F))
+        x = base + (counters + np.uint64(1)) * _GOLD
         z = (x ^ (x >> np.uint64(30))) * _M1
         z = (z ^ (z >> np.uint64(27))) * _M2
         z = z ^ (z >> np.uint64(31))
     u = (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
     return u + 0.5 / 9007199254740992.0  # strictly inside (0, 1)
+
+
+def splitmix_uniform(seed: int, stream: int, count: int) -> np.ndarray:
+    """`count` uniforms in (0, 1) from one counter-based splitmix64 stream."""
+    return splitmix_uniform_grid(seed, stream, np.arange(count, dtype=np.uint64))
 
 
 def splitmix_normal(seed: int, stream: int, count: int) -> np.ndarray:
@@ -282,10 +287,20 @@ def make_projectors(prob: Problem, basis: BasisLayout) -> np.ndarray:
     return beta
 
 
-def make_wavefunctions(prob: Problem, basis: BasisLayout, n_bands: int, seed_stream: int = 7) -> np.ndarray:
-    """C0[k, b, g] = complex Gaussian / (1 + |k+G|^2 / 2); padding zero."""
+def make_wavefunctions(prob: Problem, basis: BasisLayout, n_bands: int, seed_stream: int = 7,
+                       band_offset: int = 0) -> np.ndarray:
+    """C0[k, b, g] = complex Gaussian / (1 + |k+G|^2 / 2); padding zero.
+
+    Every (k, band) draws from its own stream, so band b has the same
+    coefficients however many bands are generated (bands start at band_offset)."""
     nk, n_tot = basis.fft_index.shape
-    C = splitmix_complex_normal(prob.seed, seed_stream, nk * n_bands * n_tot).reshape(nk, n_bands, n_tot)
+    kk = np.arange(nk, dtype=np.uint64)[:, None, None]
+    bb = (np.arange(n_bands, dtype=np.uint64) + np.uint64(band_offset))[None, :, None]
+    gg = np.arange(n_tot, dtype=np.uint64)[None, None, :]
+    sid = (np.uint64(seed_stream) << np.uint64(40)) + (kk << np.uint64(20)) + bb
+    u = [splitmix_uniform_grid(prob.seed, sid * np.uint64(4) + np.uint64(j), gg) for j in range(4)]
+    nrm = lambda a, b: np.sqrt(-2.0 * np.log(a)) * np.cos((2.0 * np.pi) * b)  # noqa: E731
+    C = nrm(u[0], u[1]) + 1j * nrm(u[2], u[3])
     damp = 1.0 / (1.0 + basis.ke)  # |k+G|^2 / 2 = ke
     C = C * damp[:, None, :]
     for ik in range(nk):

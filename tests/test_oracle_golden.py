@@ -1,0 +1,80 @@
+"""The CPU oracle against golden fixtures produced by running the reference itself.
+
+Pins the oracle: H.psi (KE + local potential + nonlocal) within 1e-12 relative
+and Davidson eigenvalues within 1e-10 Ha of the reference on the same inputs;
+the basis layout (n, fft_index) exactly.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import davidson as od
+from oracle import hpsi as oh
+from qimpy_gb300 import workloads as wl
+from qimpy_gb300.checksums import band_checksums
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, f"{name}.npz"))
+
+
+def _problem(name, nb):
+    p = wl.get(name)
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape)
+    return p, b, wl.make_projectors(p, b), wl.make_wavefunctions(p, b, nb)
+
+
+@pytest.mark.parametrize("name", ["tiny_fcc", "tiny_ortho", "si2", "si64", "cu32"])
+def test_basis_layout_matches_reference(name):
+    g = _load(name)
+    p = wl.get(name)
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape)
+    assert np.array_equal(b.n, g["n"])
+    assert np.array_equal(b.fft_index, g["fft_index"])
+    assert np.allclose(b.ke[:, :8], g["ke_ref"], rtol=1e-13, atol=0)
+    assert np.allclose(p.Gbasis, g["Gbasis_ref"], rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["tiny_fcc", "tiny_ortho"])
+def test_oracle_hpsi_full_arrays(name):
+    g = _load(name)
+    nb = int(g["hpsi_bands"])
+    p, b, beta, C = _problem(name, nb)
+    assert np.array_equal(C, g["C0"]) and np.array_equal(p.V_r, g["V_r"]) and np.array_equal(beta, g["beta"])
+    HC = oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, p.D_all(), C)
+    assert np.abs(HC - g["hpsi"]).max() <= 1e-12 * np.abs(g["hpsi"]).max()
+    proj = oh.project(beta, C)
+    assert np.abs(proj - g["proj"]).max() <= 1e-12 * np.abs(g["proj"]).max()
+
+
+@pytest.mark.parametrize("name", ["si2", "si64", "cu32"])
+def test_oracle_hpsi_checksums(name):
+    g = _load(name)
+    nb = int(g["hpsi_bands"])
+    p, b, beta, C = _problem(name, nb)
+    HC = oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, p.D_all(), C)
+    cs = band_checksums(HC, b.n)
+    assert np.abs(cs - g["hpsi_checksums"]).max() <= 1e-12 * np.abs(g["hpsi_checksums"]).max()
+    for (k, bb), ref in zip(g["hpsi_sample_kb"], g["hpsi_sample"]):
+        assert np.abs(HC[k, bb] - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["tiny_fcc", "tiny_ortho", "si2"])
+def test_oracle_davidson_eigenvalues(name):
+    g = _load(name)
+    pw = wl.get(name)
+    p, b, beta, C = _problem(name, pw.n_bands + pw.n_bands_extra)
+    H = lambda X: oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, p.D_all(), X)  # noqa: E731
+    r = od.davidson(H, od.orthonormalize(C), b.ke, b.n, p.n_bands, 300, float(g["eig_threshold"]))
+    assert r.converged
+    assert np.abs(r.eig[:, : p.n_bands] - g["eig"][:, : p.n_bands]).max() < 1e-10
+    assert r.iterations == int(g["davidson_iterations"])
+
+
+def test_oracle_davidson_rejects_oversized_subspace():
+    p, b, beta, C = _problem("tiny_fcc", 60)
+    with pytest.raises(ValueError):
+        od.davidson(lambda X: X, C, b.ke, b.n, 50)
