@@ -123,6 +123,31 @@ int qgb_apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out
                         unsigned flags, void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * qgb_apply_potential without a workspace argument, for callers that cannot
+ * allocate device memory: host codes whose device memory belongs to an outer
+ * framework that forbids allocations by plugins, or code running where
+ * cudaMalloc is not allowed (inside a stream capture, or a serving loop with a
+ * fixed memory budget).  No counterpart in the reference.
+ *
+ * Same arguments, flags and results as qgb_apply_potential; the slab-plane
+ * scratch is a fixed file-scope device array of qgb_static_scratch_bytes()
+ * (32 MiB) that every GPU loading the library holds until exit.  Bands are
+ * processed in as many chunks as that scratch needs; a sphere for which even
+ * one band does not fit is rejected with QGB_ERR_WORKSPACE.  The function
+ * calls no allocator.
+ *   - The first call on a device looks up the array's device address (once per
+ *     device, with that device current); make that first call before any
+ *     stream capture.
+ *   - All calls share the one array and it keeps the previous call's contents;
+ *     nothing in it needs to start at zero (every plane is written before it is
+ *     read within a call).  Calls that overlap on the GPU (different streams,
+ *     or host threads without ordering) race on the array: serialise them.
+ */
+int qgb_apply_potential_static(const qgb_sphere* s, int dtype, const void* C, void* out, int nb,
+                               unsigned flags, void* stream);
+size_t qgb_static_scratch_bytes(void);
+
+/*
  * projT[k][b][p] = sum_g conj(beta[k][p][g]) C[k][b][g]  (replaces Wavefunction.proj
  * = beta ^ C, qimpy/dft/electrons/_wavefunction.py:106-123 and
  * _wavefunction_dot.py:18-107).

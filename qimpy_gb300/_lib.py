@@ -58,6 +58,9 @@ _SIGS = {
                                    ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
                                    ct.c_size_t, ct.c_void_p]),
     "qgb_fma_burn": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "qgb_apply_potential_static": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
+                                              ct.c_uint, ct.c_void_p]),
+    "qgb_static_scratch_bytes": (ct.c_size_t, []),
 }
 
 #: Every symbol the header declares (checked by the CPU tests).
