@@ -179,6 +179,35 @@ int qgb_hamiltonian(const qgb_sphere* s, int dtype, const void* C, void* HC, int
 size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int dtype);
 
 /*
+ * Mixed-precision nonlocal term on the tcgen05 tensor cores (split-BF16x3,
+ * FP32 accumulation):  projT = <beta|C>  and  HC += beta (D projT), complex64
+ * (replaces C.proj and beta @ (D_all @ C.proj),
+ * qimpy/dft/electrons/_wavefunction.py:106-123 and _hamiltonian.py:22-24).
+ *   qgb_beta_split      once per basis: beta complex64 [nk][P][n_tot] -> bf16
+ *                       hi/lo operands in `out` (qgb_beta_split_bytes).
+ *   qgb_apply_nonlocal_tc  per call; D complex64 per-atom blocks; `workspace`
+ *                       of qgb_nonlocal_tc_workspace_bytes; `dev_error` is a
+ *                       device int that a kernel sets nonzero (and keeps) if a
+ *                       bounded pipeline wait timed out.
+ */
+size_t qgb_beta_split_bytes(int nk, int P, int n_tot);
+int qgb_beta_split(const void* beta, int nk, int P, int n_tot, void* out, size_t out_bytes, void* stream);
+size_t qgb_nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot);
+int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, int pa, const void* C, void* HC,
+                          void* projT, int nk, int nb, int n_tot, void* workspace, size_t workspace_bytes,
+                          int* dev_error, void* stream);
+
+/*
+ * The underlying real GEMM, exposed for verification: D (FP32 [M][N], N <= 64)
+ * = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with bf16 K-major A [M][lda],
+ * B [N][ldb] (lda, ldb multiples of 8).  workspace >= ceil(M/128)*128*64*4 B.
+ * No reference counterpart (test aid for the tensor-core path).
+ */
+int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N,
+                       int K, int lda, int ldb, float* D, int* dev_error, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
+/*
  * Diagnostic: `blocks` x `threads` threads each run 8 independent FMA chains
  * of 8*iters steps (64*iters FMAs = 128*iters flops per thread).  Timed by
  * the caller; gives the FP64/FP32 CUDA-core peak used as a roofline

@@ -61,6 +61,15 @@ _SIGS = {
     "qgb_apply_potential_static": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
                                               ct.c_uint, ct.c_void_p]),
     "qgb_static_scratch_bytes": (ct.c_size_t, []),
+    "qgb_beta_split_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int]),
+    "qgb_beta_split": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_nonlocal_tc_workspace_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int, ct.c_int]),
+    "qgb_apply_nonlocal_tc": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                         ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_size_t,
+                                         ct.c_void_p, ct.c_void_p]),
+    "qgb_tc_gemm_bf16x3": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
+                                      ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                      ct.c_size_t, ct.c_void_p]),
 }
 
 #: Every symbol the header declares (checked by the CPU tests).

@@ -40,6 +40,13 @@ int apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int 
 #ifdef QGB_DEBUG_CHECKS
 int debug_violation(unsigned long long* out4);
 #endif
+size_t beta_split_bytes(int nk, int P, int n_tot);
+int beta_split(const void* beta, int nk, int P, int n_tot, void* out, size_t out_bytes, cudaStream_t st);
+size_t nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot);
+int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
+                int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, cudaStream_t st);
+int tc_gemm_test(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N, int K,
+                 int lda, int ldb, float* D, int* err, void* ws, size_t ws_bytes, cudaStream_t st);
 
 }  // namespace qgb
 
@@ -125,5 +132,29 @@ int qgb_hamiltonian(const qgb_sphere* s, int dtype, const void* C, void* HC, int
 #ifdef QGB_DEBUG_CHECKS
 int qgb_debug_violation(unsigned long long* out4) { return qgb::debug_violation(out4); }
 #endif
+
+size_t qgb_beta_split_bytes(int nk, int P, int n_tot) { return beta_split_bytes(nk, P, n_tot); }
+
+int qgb_beta_split(const void* beta, int nk, int P, int n_tot, void* out, size_t out_bytes, void* stream) {
+  return beta_split(beta, nk, P, n_tot, out, out_bytes, static_cast<cudaStream_t>(stream));
+}
+
+size_t qgb_nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot) {
+  return nonlocal_tc_workspace_bytes(nk, P, nb, n_tot);
+}
+
+int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, int pa, const void* C, void* HC,
+                          void* projT, int nk, int nb, int n_tot, void* workspace, size_t workspace_bytes,
+                          int* dev_error, void* stream) {
+  return nonlocal_tc(beta_split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, workspace, workspace_bytes,
+                     dev_error, static_cast<cudaStream_t>(stream));
+}
+
+int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N,
+                       int K, int lda, int ldb, float* D, int* dev_error, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  return tc_gemm_test(a_hi, a_lo, b_hi, b_lo, M, N, K, lda, ldb, D, dev_error, workspace, workspace_bytes,
+                      static_cast<cudaStream_t>(stream));
+}
 
 }  // extern "C"

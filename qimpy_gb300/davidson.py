@@ -7,8 +7,9 @@ eigenvalue change).  Additions:
 
 * an optional residual-norm stop (max_b ||H psi_b - eps_b psi_b|| over the
   first n_bands, in FP64) beside the reference's eigenvalue-change stop;
-* ``refine_fp64``: one FP64 Rayleigh-Ritz sweep (FP64 H.psi, Cholesky
-  orthonormalisation and eigh) on the vectors of a mixed-precision solve.
+* ``refine_fp64``: FP64 refinement of a mixed-precision solve (Cholesky
+  orthonormalisation, then FP64 Davidson sweeps: FP64 H.psi, Rayleigh-Ritz,
+  residual expansion, expanded Rayleigh-Ritz).
 """
 from __future__ import annotations
 
@@ -52,7 +53,13 @@ class Davidson:
         self.n_iterations = n_iterations
         self.eig_threshold = eig_threshold
         self.residual_threshold = residual_threshold
-        self._norm_cut = float(np.sqrt(electrons.basis.n_tot * 1e-15))  # _davidson.py:56-58
+        # Expansion vectors shorter than this are treated as null and re-randomised
+        # (_davidson.py:56-58, 101-115).  The reference's round-off estimate
+        # sqrt(n_tot * 1e-15) is also a floor on reachable residuals, so a
+        # residual target below it lowers the cut to 1% of the target.
+        self._norm_cut = float(np.sqrt(electrons.basis.n_tot * 1e-15))
+        if residual_threshold is not None:
+            self._norm_cut = min(self._norm_cut, 0.01 * residual_threshold)
         self._i_iter = 0
 
     def precondition(self, Cerr: Wavefunction, KEref: torch.Tensor) -> Wavefunction:
@@ -103,9 +110,6 @@ class Davidson:
             HC_sel = HC.bands(n_eigs_done) if n_eigs_done else HC
             KEref = C_sel.band_ke()
             R = HC_sel - C_sel * eig_sel.to(C_sel.coeff.real.dtype)
-            if self.residual_threshold is not None:
-                rn = R.band_norm()[:, : max(0, n_bands - n_eigs_done)]
-                res_max = float(rn.max()) if rn.numel() else 0.0
             Cexp = self.precondition(R, KEref)
             norm_exp = Cexp.band_norm()
             self._regularize(Cexp, norm_exp, self._i_iter)
@@ -134,26 +138,36 @@ class Davidson:
             pending = torch.where((d > self.eig_threshold).any(dim=0))[0]
             n_eigs_done = int(pending[0]) if len(pending) else n_bands
             converged = n_eigs_done >= n_bands
-            if self.residual_threshold is not None:
-                converged = converged and res_max < self.residual_threshold
-                if not converged and n_eigs_done >= n_bands:
-                    n_eigs_done = 0  # eigenvalues settled but residuals not yet: keep all active
+            if converged and self.residual_threshold is not None:
+                # HC is carried by rotations and drifts from H C over many
+                # iterations; test residuals against a fresh H C.
+                HC = el.hamiltonian(el.C)
+                res = (HC - el.C * el.eig[..., None].to(el.C.coeff.real.dtype)).band_norm()
+                res_max = float(res[:, :n_bands].max())
+                if res_max >= self.residual_threshold:
+                    converged = False
+                    n_eigs_done = 0  # eigenvalues settled, residuals not yet: keep all bands active
             if converged:
                 break
         self._HC = HC
         return DavidsonStats(self._i_iter, converged, el.deig_max, res_max, el.hpsi_band_count - hpsi0)
 
 
-def refine_fp64(el_mixed: Electrons, el_fp64: Electrons, C: Optional[Wavefunction] = None):
-    """FP64 Rayleigh-Ritz sweep on mixed-precision eigenvectors.
+def refine_fp64(el_mixed: Electrons, el_fp64: Electrons, C: Optional[Wavefunction] = None,
+                eig_threshold: float = 1e-8, max_sweeps: int = 8):
+    """FP64 refinement of mixed-precision eigenvectors.
 
     Upcasts the vectors to complex128, orthonormalises them (Cholesky, FP64),
-    applies the FP64 Hamiltonian and diagonalises C^H H C.  Returns
-    (eigenvalues (nk, nb) FP64, refined FP64 Wavefunction)."""
+    then runs FP64 Davidson sweeps (Rayleigh-Ritz with the FP64 Hamiltonian,
+    preconditioned residual expansion, expanded Rayleigh-Ritz) until the
+    eigenvalues change by less than `eig_threshold` (at most `max_sweeps`).
+    FP32 H.psi leaves eigenvalues with noise near eps_f32 * Ecut (~1e-6 Ha);
+    the FP64 sweeps remove it.  Returns (eigenvalues (nk, nb) FP64, refined FP64
+    Wavefunction); el_fp64 holds the refined state and `el_fp64.last_refine`
+    the sweep statistics."""
     C = C or el_mixed.C
     C64 = Wavefunction(el_fp64.basis, coeff=C.coeff.to(torch.complex128))
     C64.constrain()
-    C64 = C64.orthonormalize()
-    HC = el_fp64.hamiltonian(C64)
-    E, V = torch.linalg.eigh((C64 ^ HC).wait())
-    return E, C64 @ V
+    el_fp64.C = C64.orthonormalize()
+    el_fp64.last_refine = Davidson(el_fp64, n_iterations=max_sweeps, eig_threshold=eig_threshold)()
+    return el_fp64.eig, el_fp64.C

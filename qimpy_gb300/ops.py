@@ -114,3 +114,58 @@ def hamiltonian(sphere: DeviceSphere, C: torch.Tensor, beta: torch.Tensor | None
                                           nb, bptr, dptr, n_atoms, pa, pptr, ws.data_ptr(), ws.numel(),
                                           _stream()), "hamiltonian")
     return out, projT
+
+
+# ---------------------------------------------------------------------------
+# Mixed precision: tensor-core (tcgen05, split-BF16x3) nonlocal term
+# ---------------------------------------------------------------------------
+
+_ERR_WORDS: dict = {}
+
+
+def device_error_word(device) -> torch.Tensor:
+    """Per-device int32 that tensor-core kernels set nonzero if a bounded
+    pipeline wait times out (sticky until cleared by the caller)."""
+    dev = torch.device(device)
+    key = dev.index if dev.index is not None else torch.cuda.current_device()
+    if key not in _ERR_WORDS:
+        _ERR_WORDS[key] = torch.zeros(1, dtype=torch.int32, device=dev)
+    return _ERR_WORDS[key]
+
+
+def beta_split(beta: torch.Tensor) -> torch.Tensor:
+    """Once per basis: complex64 projectors (nk, P, n_tot) -> bf16 hi/lo operands."""
+    if beta.dtype != torch.complex64 or not beta.is_cuda or not beta.is_contiguous():
+        raise TypeError("beta must be a contiguous complex64 CUDA tensor")
+    nk, P, n_tot = beta.shape
+    nbytes = int(_lib.lib().qgb_beta_split_bytes(nk, P, n_tot))
+    out = torch.empty(nbytes, dtype=torch.uint8, device=beta.device)
+    _lib.check(_lib.lib().qgb_beta_split(beta.data_ptr(), nk, P, n_tot, out.data_ptr(), nbytes, _stream()),
+               "beta_split")
+    return out
+
+
+def apply_nonlocal_tc(split: torch.Tensor, D_blocks: torch.Tensor, C: torch.Tensor, HC: torch.Tensor,
+                      projT: torch.Tensor | None = None, ws: torch.Tensor | None = None):
+    """HC += beta D <beta|C> on the tensor cores (complex64); returns projT (nk, nb, P)."""
+    nk, nb, n_tot = C.shape
+    n_atoms, pa, _ = D_blocks.shape
+    P = n_atoms * pa
+    if C.dtype != torch.complex64 or HC.dtype != torch.complex64 or D_blocks.dtype != torch.complex64:
+        raise TypeError("tensor-core nonlocal needs complex64 C, HC and D")
+    projT = torch.empty((nk, nb, P), dtype=torch.complex64, device=C.device) if projT is None else projT
+    if ws is None:
+        ws = workspace(int(_lib.lib().qgb_nonlocal_tc_workspace_bytes(nk, P, nb, n_tot)), C.device)
+    err = device_error_word(C.device)
+    _lib.check(_lib.lib().qgb_apply_nonlocal_tc(split.data_ptr(), D_blocks.data_ptr(), n_atoms, pa, C.data_ptr(),
+                                                HC.data_ptr(), projT.data_ptr(), nk, nb, n_tot, ws.data_ptr(),
+                                                ws.numel(), err.data_ptr(), _stream()), "apply_nonlocal_tc")
+    return projT
+
+
+def hamiltonian_mixed(sphere: DeviceSphere, C: torch.Tensor, split: torch.Tensor, D_blocks: torch.Tensor,
+                      out: torch.Tensor | None = None, projT: torch.Tensor | None = None):
+    """Mixed-precision H.psi: FP32 KE + local potential, tensor-core nonlocal."""
+    out = apply_potential(sphere, C, out=out, add_ke=True)
+    projT = apply_nonlocal_tc(split, D_blocks, C, out, projT)
+    return out, projT
