@@ -198,6 +198,18 @@ int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, in
                           int* dev_error, void* stream);
 
 /*
+ * Mixed-precision H C (complex64): FP32 KE + local potential (as
+ * qgb_apply_potential with QGB_ADD_KE), then the tensor-core nonlocal term
+ * (qgb_apply_nonlocal_tc); replaces Electrons.hamiltonian,
+ * qimpy/dft/electrons/_hamiltonian.py:7-29, in the mixed form.  beta_split
+ * comes from qgb_beta_split; workspace of qgb_hamiltonian_mixed_workspace_bytes.
+ */
+size_t qgb_hamiltonian_mixed_workspace_bytes(const qgb_sphere* s, int nb, int P);
+int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, const void* beta_split,
+                          const void* D, int n_atoms, int pa, void* projT, void* workspace, size_t workspace_bytes,
+                          int* dev_error, void* stream);
+
+/*
  * The underlying real GEMM, exposed for verification: D (FP32 [M][N], N <= 64)
  * = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with bf16 K-major A [M][lda],
  * B [N][ldb] (lda, ldb multiples of 8).  workspace >= ceil(M/128)*128*64*4 B.

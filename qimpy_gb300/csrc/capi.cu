@@ -150,6 +150,28 @@ int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, in
                      dev_error, static_cast<cudaStream_t>(stream));
 }
 
+size_t qgb_hamiltonian_mixed_workspace_bytes(const qgb_sphere* s, int nb, int P) {
+  if (!s || nb < 0 || P < 0) return 0;
+  const size_t nl = (nonlocal_tc_workspace_bytes(s->nk, P, nb, s->n_tot) + 255) / 256 * 256;
+  return nl + plane_bytes_per_band(*s, QGB_F32) * static_cast<size_t>(nb);
+}
+
+int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, const void* beta_split,
+                          const void* D, int n_atoms, int pa, void* projT, void* workspace, size_t workspace_bytes,
+                          int* dev_error, void* stream) {
+  int rc = validate_sphere(s, QGB_F32);
+  if (rc) return rc;
+  if (C == HC) return fail(QGB_ERR_INVALID, "C and HC must not alias");
+  const int P = n_atoms * pa;
+  const size_t nl = P > 0 ? (nonlocal_tc_workspace_bytes(s->nk, P, nb, s->n_tot) + 255) / 256 * 256 : 0;
+  if (workspace_bytes < nl) return fail(QGB_ERR_WORKSPACE, "workspace too small for the nonlocal term");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* ws = static_cast<char*>(workspace);
+  rc = apply_potential(s, QGB_F32, C, HC, nb, QGB_ADD_KE, ws + nl, workspace_bytes - nl, st);
+  if (rc || P == 0) return rc;
+  return nonlocal_tc(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl, dev_error, st);
+}
+
 int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N,
                        int K, int lda, int ldb, float* D, int* dev_error, void* workspace, size_t workspace_bytes,
                        void* stream) {

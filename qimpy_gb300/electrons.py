@@ -106,6 +106,9 @@ class Ions:
             self.beta = beta.to(basis.device, basis.dtype).contiguous()
             self.D = D_atom.to(basis.device, basis.dtype).contiguous()
             self.n_projectors = int(beta.shape[1])
+        # Mixed form: bf16 hi/lo projector operands for the tensor-core GEMMs.
+        self.beta_split = (ops.beta_split(self.beta)
+                           if self.beta is not None and basis.dtype == torch.complex64 else None)
         self.beta_version = 0
 
     def D_all(self) -> torch.Tensor:
@@ -248,10 +251,14 @@ class Electrons:
         self.hpsi_band_count = 0  # band-applications performed (all k)
 
     def hamiltonian(self, C: Wavefunction) -> Wavefunction:
-        """HC in one C-ABI call (fused KE + local potential, then nonlocal GEMMs)."""
+        """HC in one C-ABI call: fused KE + local potential, then the nonlocal
+        term (FP64: ZGEMMs; mixed: tcgen05 split-BF16x3 GEMMs)."""
         ions = self.ions
-        beta = ions.beta if ions.n_projectors else None
-        HC, projT = ops.hamiltonian(self.basis.sphere, C.coeff, beta, ions.D)
+        if self.basis.dtype == torch.complex64:
+            HC, projT = ops.hamiltonian_mixed(self.basis.sphere, C.coeff, ions.beta_split, ions.D)
+        else:
+            beta = ions.beta if ions.n_projectors else None
+            HC, projT = ops.hamiltonian(self.basis.sphere, C.coeff, beta, ions.D)
         if projT is not None:
             C._projT, C._proj_version = projT, ions.beta_version
         self.hpsi_band_count += C.n_bands() * self.basis.nk

@@ -163,9 +163,28 @@ def apply_nonlocal_tc(split: torch.Tensor, D_blocks: torch.Tensor, C: torch.Tens
     return projT
 
 
-def hamiltonian_mixed(sphere: DeviceSphere, C: torch.Tensor, split: torch.Tensor, D_blocks: torch.Tensor,
-                      out: torch.Tensor | None = None, projT: torch.Tensor | None = None):
-    """Mixed-precision H.psi: FP32 KE + local potential, tensor-core nonlocal."""
-    out = apply_potential(sphere, C, out=out, add_ke=True)
-    projT = apply_nonlocal_tc(split, D_blocks, C, out, projT)
+def hamiltonian_mixed(sphere: DeviceSphere, C: torch.Tensor, split: torch.Tensor | None,
+                      D_blocks: torch.Tensor | None, out: torch.Tensor | None = None,
+                      projT: torch.Tensor | None = None, ws: torch.Tensor | None = None):
+    """Mixed-precision H.psi in one C-ABI call: FP32 KE + local potential,
+    tensor-core (split-BF16x3) nonlocal.  Returns (HC, projT)."""
+    nb = _check_wf(sphere, C)
+    if sphere.cdtype != torch.complex64:
+        raise TypeError("hamiltonian_mixed needs a complex64 sphere")
+    out = torch.empty_like(C) if out is None else out
+    if split is None or D_blocks is None:
+        n_atoms = pa = P = 0
+        sptr = dptr = pptr = 0
+    else:
+        n_atoms, pa, _ = D_blocks.shape
+        P = n_atoms * pa
+        projT = torch.empty((C.shape[0], nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
+        sptr, dptr, pptr = split.data_ptr(), D_blocks.data_ptr(), projT.data_ptr()
+    if ws is None:
+        ws = workspace(int(_lib.lib().qgb_hamiltonian_mixed_workspace_bytes(ct.byref(sphere.struct), nb, P)),
+                       C.device)
+    err = device_error_word(C.device)
+    _lib.check(_lib.lib().qgb_hamiltonian_mixed(ct.byref(sphere.struct), C.data_ptr(), out.data_ptr(), nb, sptr,
+                                                dptr, n_atoms, pa, pptr, ws.data_ptr(), ws.numel(), err.data_ptr(),
+                                                _stream()), "hamiltonian_mixed")
     return out, projT
