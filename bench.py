@@ -52,6 +52,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--eig-reps", type=int, default=3)
     ap.add_argument("--forms", default="fp64,mixed", help="precision forms to run (profiling aid)")
+    ap.add_argument("--plane-budget-mb", type=int, default=0, help="slab-plane workspace cap (0 = default)")
     ap.add_argument("--no-eigensolve", action="store_true")
     return ap.parse_args()
 
@@ -227,14 +228,15 @@ def run_gb300(args, rank, ws, local):
         HC = torch.empty_like(C)
         projT = torch.empty((p.nk, block, p.n_projectors), dtype=cdt, device=dev)
         work = torch.empty_like(projT)
+        if args.plane_budget_mb:
+            ds.plane_budget_bytes = args.plane_budget_mb << 20
         wsp = ops.workspace(ds.workspace_bytes(block), dev)
         mixed = cdt == torch.complex64
         if mixed:  # tensor-core nonlocal: projector operands split once per basis
             split = ops.beta_split(beta)
             ws_nl = ops.workspace(int(_lib.lib().qgb_nonlocal_tc_workspace_bytes(p.nk, p.n_projectors, block,
                                                                                  b.n_tot)), dev)
-            ws_ham = ops.workspace(int(_lib.lib().qgb_hamiltonian_mixed_workspace_bytes(
-                ct.byref(ds.struct), block, p.n_projectors)), dev)
+            ws_ham = ops.workspace(ds.hamiltonian_mixed_workspace_bytes(block, p.n_projectors), dev)
         st = torch.cuda.current_stream()
 
         C_blk = [C[:, s0:s1].contiguous() for (s0, s1) in blocks]

@@ -205,6 +205,141 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
   }
 }
 
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The x-pass middle step on one item: inverse L1-point DFT, multiply by V,
+// forward L1-point DFT, forward-pass twiddles; data at sm[p + j*ld], V at
+// Vp[j * vstride] (global or shared), twiddles at sm[Wx + j*L2 + a].
+template <typename T, int R, typename VPtr>
+__device__ __forceinline__ void xmid_item(cplx_t<T>* sm, int p, int ld, VPtr Vp, size_t vstride, int Wx, int L2,
+                                          int a) {
+  using C2 = cplx_t<T>;
+  T re[R], im[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const C2 v = sm[p + j * ld];
+    re[j] = v.x;
+    im[j] = v.y;
+  }
+  Codelet<R, +1>::run(re, im);
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const T vv = Vp[j * vstride];
+    re[j] *= vv;
+    im[j] *= vv;
+  }
+  Codelet<R, -1>::run(re, im);
+  if (L2 > 1) {
+#pragma unroll
+    for (int j = 1; j < R; ++j) {
+      const C2 w = sm[Wx + j * L2 + a];
+      const T xr = re[j] * w.x + im[j] * w.y;
+      const T xi = im[j] * w.x - re[j] * w.y;
+      re[j] = xr;
+      im[j] = xi;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < R; ++j) sm[p + j * ld] = mk<T>(re[j], im[j]);
+}
+
+template <typename T, typename VPtr>
+__device__ __forceinline__ void xmid_dispatch(int L1, cplx_t<T>* sm, int p, int ld, VPtr Vp, size_t vstride, int Wx,
+                                              int L2, int a) {
+  switch (L1) {
+    case 1: xmid_item<T, 1>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 2: xmid_item<T, 2>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 3: xmid_item<T, 3>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 4: xmid_item<T, 4>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 5: xmid_item<T, 5>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 6: xmid_item<T, 6>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 7: xmid_item<T, 7>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 8: xmid_item<T, 8>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 9: xmid_item<T, 9>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 10: xmid_item<T, 10>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 12: xmid_item<T, 12>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 14: xmid_item<T, 14>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 15: xmid_item<T, 15>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    case 16: xmid_item<T, 16>(sm, p, ld, Vp, vstride, Wx, L2, a); break;
+    default: break;
+  }
+}
+
+// x-pass with asynchronous staging (FP32, N2 % 4 == 0): the slab rows and the
+// CTA's V slice are copied to shared memory with cp.async (no register
+// staging); V streams in while the first inverse pass runs, so the middle
+// step reads only shared memory.  Shared layout: pencils [N0][ldx = N2 + 2]
+// complex, W_x [N0] complex, V slice [N0][N2] real.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_xpass_async(const qgb_sphere s, LocalParams lp,
+                                                          cplx_t<T>* __restrict__ planes) {
+  using C2 = cplx_t<T>;
+  const int r1 = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
+  const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 2;
+  const int L1 = s.L1[0], L2 = s.L2[0];
+  const int lim = N0 * ld, Wx = lim;
+  C2* sm = smem_c<T>();
+  T* Vs = reinterpret_cast<T*>(sm + ((Wx + N0 + 1) & ~1));  // 16-byte aligned for cp.async
+  const C2* tw = static_cast<const C2*>(s.twiddle);
+  load_twiddles<T>(Wx, tw + s.tw_off[0], N0);
+  const C2 zero = mk<T>(T(0), T(0));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int r = warp; r < N0; r += nwarps)
+    for (int c = lane; c < N2; c += 32) sm[r * ld + c] = zero;
+  __syncthreads();
+
+  const int nslabs = s.n_slabs[k];
+  const int* i0 = s.slab_i0 + k * s.max_slabs;
+  const size_t plane = static_cast<size_t>(N1) * N2;
+  C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2;
+  // Group 1: slab rows (16 B = 2 complex per copy).
+  const int cpr = N2 / 2;  // copies per row
+  for (int it = threadIdx.x; it < nslabs * cpr; it += blockDim.x) {
+    const int sl = it / cpr, c = 2 * (it - sl * cpr);
+    cp_async16(sm + i0[sl] * ld + c, base + sl * plane + c);
+  }
+  cp_async_commit();
+  // Group 2: V slice V[p0][r1][*] for all p0 (16 B = 4 reals per copy).
+  const T* V = static_cast<const T*>(s.V);
+  const int vpr = N2 / 4;
+  for (int it = threadIdx.x; it < N0 * vpr; it += blockDim.x) {
+    const int p0 = it / vpr, c = 4 * (it - p0 * vpr);
+    cp_async16(Vs + p0 * N2 + c, V + (static_cast<size_t>(p0) * N1 + r1) * N2 + c);
+  }
+  cp_async_commit();
+  cp_async_wait<1>();
+  __syncthreads();
+
+  if (L2 > 1) {
+    run_pass<T, +1>(L2, Pass{nullptr, 0, N2, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int it = threadIdx.x; it < N2 * L2; it += blockDim.x) {
+    const int a = it / N2;
+    const int c = it - a * N2;
+    xmid_dispatch<T>(L1, sm, c + a * L1 * ld, ld, Vs + a * L1 * N2 + c, static_cast<size_t>(N2), Wx, L2, a);
+  }
+  __syncthreads();
+  if (L2 > 1) {
+    run_pass<T, -1>(L2, Pass{nullptr, 0, N2, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
+    __syncthreads();
+  }
+  for (int sl = warp; sl < nslabs; sl += nwarps) {
+    C2* dst = base + sl * plane;
+    const int x = i0[sl];
+    for (int c = lane; c < N2; c += 32) dst[c] = sm[x * ld + c];
+  }
+}
+
 // C and out may alias (in-place apply): no __restrict__ on them.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, LocalParams lp,
@@ -315,6 +450,14 @@ size_t plane_smem_bytes(const qgb_sphere& s, int dtype) {
   return std::max(yz, x);
 }
 
+// The asynchronous x-pass: FP32 with 16-byte aligned rows of V and of the planes.
+static bool xpass_async_ok(const qgb_sphere& s, int dtype) { return dtype == QGB_F32 && s.N[2] % 4 == 0; }
+
+static size_t xpass_async_smem_bytes(const qgb_sphere& s) {
+  const size_t cplx = (static_cast<size_t>(s.N[0]) * (s.N[2] + 2) + s.N[0] + 1) & ~static_cast<size_t>(1);
+  return cplx * 8 + static_cast<size_t>(s.N[0]) * s.N[2] * 4;
+}
+
 int validate_sphere(const qgb_sphere* s, int dtype) {
   if (s == nullptr) return fail(QGB_ERR_INVALID, "sphere descriptor is NULL");
   if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
@@ -332,7 +475,7 @@ int validate_sphere(const qgb_sphere* s, int dtype) {
   if (!s->n || !s->n_slabs || !s->slab_start || !s->slab_i0 || !s->yz || !s->row_start ||
       !s->rows || !s->twiddle || !s->ke || !s->V)
     return fail(QGB_ERR_INVALID, "sphere descriptor has a NULL table");
-  if (plane_smem_bytes(*s, dtype) > 227 * 1024)
+  if (plane_smem_bytes(*s, dtype) > 227 * 1024 || (xpass_async_ok(*s, dtype) && xpass_async_smem_bytes(*s) > 227 * 1024))
     return fail(QGB_ERR_UNSUPPORTED, "grid %dx%dx%d needs %zu B of shared memory per plane (max 227 KB)",
                 s->N[0], s->N[1], s->N[2], plane_smem_bytes(*s, dtype));
   return QGB_OK;
@@ -350,8 +493,19 @@ static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* 
   k_ifft_yz<T><<<g1, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(C), static_cast<C2*>(planes));
   QGB_LAUNCH_CHECK("k_ifft_yz");
   const dim3 g2(s.N[1], lp.nb, s.nk);
-  k_xpass<T><<<g2, kThreads, smem, st>>>(s, lp, static_cast<C2*>(planes));
-  QGB_LAUNCH_CHECK("k_xpass");
+  if (sizeof(T) == 4 && s.N[2] % 4 == 0) {
+    const size_t smx = xpass_async_smem_bytes(s);
+    static size_t configured = 0;
+    if (smx > configured) {
+      QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_async<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
+      configured = smx;
+    }
+    k_xpass_async<T><<<g2, kThreads, smx, st>>>(s, lp, static_cast<C2*>(planes));
+    QGB_LAUNCH_CHECK("k_xpass_async");
+  } else {
+    k_xpass<T><<<g2, kThreads, smem, st>>>(s, lp, static_cast<C2*>(planes));
+    QGB_LAUNCH_CHECK("k_xpass");
+  }
   k_fft_yz_gather<T><<<g1, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(C),
                                                 static_cast<C2*>(out), static_cast<const C2*>(planes));
   QGB_LAUNCH_CHECK("k_fft_yz_gather");

@@ -175,7 +175,7 @@ struct Smem {
 };
 
 template <int BN, int STAGES, int EPI>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads)
     k_tc_gemm(const __grid_constant__ CUtensorMap mA_hi, const __grid_constant__ CUtensorMap mA_lo,
               const __grid_constant__ CUtensorMap mB_hi, const __grid_constant__ CUtensorMap mB_lo,
               const GemmArgs args) {
@@ -440,21 +440,37 @@ __global__ void k_split_beta(const float2* __restrict__ beta, int P, int n_tot, 
 // D rows m < P are Re beta_m, rows P + m are Im beta_m; columns follow the
 // band-row order of k_split_bands.
 //   Re <b_p|psi_b> = D[p][re b] + D[P+p][im b],  Im = D[p][im b] - D[P+p][re b]
+// Threads run along the band columns of a partial row (coalesced reads).
+// Block (32, 8): threadIdx.x runs along bands, threadIdx.y strides the splits;
+// the 8 partial sums of each band are combined in shared memory.
 __global__ void k_reduce_proj(const float* __restrict__ partial, int splits, long long part_rows, int part_ld,
                               int P, int nb, int HB, float2* __restrict__ projT) {
-  const int k = blockIdx.z;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nb * P) return;
-  const int b = idx / P, p = idx - b * P;
-  const int t = b / HB, j = b - t * HB;
-  const int c_re = t * 2 * HB + j, c_im = c_re + HB;
+  __shared__ float2 acc[8][32];
+  const int k = blockIdx.z, p = blockIdx.y;
+  const int b = blockIdx.x * 32 + threadIdx.x;
   float re = 0.f, im = 0.f;
-  for (int s = 0; s < splits; ++s) {
-    const float* D = partial + (static_cast<long long>(k) * splits + s) * part_rows * part_ld;
-    re += D[static_cast<long long>(p) * part_ld + c_re] + D[static_cast<long long>(P + p) * part_ld + c_im];
-    im += D[static_cast<long long>(p) * part_ld + c_im] - D[static_cast<long long>(P + p) * part_ld + c_re];
+  if (b < nb) {
+    const int t = b / HB, j = b - t * HB;
+    const int c_re = t * 2 * HB + j, c_im = c_re + HB;
+    for (int s = threadIdx.y; s < splits; s += 8) {
+      const float* D = partial + (static_cast<long long>(k) * splits + s) * part_rows * part_ld;
+      const float* r0 = D + static_cast<long long>(p) * part_ld;
+      const float* r1 = D + static_cast<long long>(P + p) * part_ld;
+      re += r0[c_re] + r1[c_im];
+      im += r0[c_im] - r1[c_re];
+    }
   }
-  projT[(static_cast<long long>(k) * nb + b) * P + p] = make_float2(re, im);
+  acc[threadIdx.y][threadIdx.x] = make_float2(re, im);
+  __syncthreads();
+  if (threadIdx.y == 0 && b < nb) {
+    float2 sum = acc[0][threadIdx.x];
+#pragma unroll
+    for (int y = 1; y < 8; ++y) {
+      sum.x += acc[y][threadIdx.x].x;
+      sum.y += acc[y][threadIdx.x].y;
+    }
+    projT[(static_cast<long long>(k) * nb + b) * P + p] = sum;
+  }
 }
 
 // Dp[b][p] = sum_q D_atom[a][p'][q'] projT[b][a*pa + q'] (block-diagonal D),
@@ -532,6 +548,10 @@ int beta_split(const void* beta, int nk, int P, int n_tot, void* out, size_t out
   return QGB_OK;
 }
 
+// Pipeline depth per tile width: BN = 64 and 128 keep two CTAs per SM
+// (96 KB of stages), BN = 256 runs one CTA per SM with 4 stages (192 KB).
+template <int BN> constexpr int kStages = (BN == 64) ? 4 : (BN == 128 ? 3 : 4);
+
 // Band-block tile width for the nonlocal GEMMs.
 static int pick_bn(int nb) { return nb <= 32 ? 64 : (nb <= 64 ? 128 : 256); }
 
@@ -599,15 +619,15 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
   g1.part_ld = static_cast<int>(W.rowsB);
   g1.part_rows = (2LL * P + BM - 1) / BM * BM;
   g1.err = err;
-  int rc = launch<BN, (BN == 256 ? 4 : 6), EPI_PARTIAL>(
+  int rc = launch<BN, kStages<BN>, EPI_PARTIAL>(
       Operand{a_hi, a_lo, 2LL * P, BL.ldA, 2LL * P * BL.ldA}, Operand{b_hi, b_lo, W.rowsB, W.ldB, W.rowsB * W.ldB},
       n_tot, nk, g1, st);
   if (rc) return rc;
   // 3. Reduce -> projT; apply D; build the back-projection operand.
   {
-    dim3 grid((nb * P + 255) / 256, 1, nk);
-    k_reduce_proj<<<grid, 256, 0, st>>>(partial, W.splits, g1.part_rows, g1.part_ld, P, nb, W.HB,
-                                        static_cast<float2*>(projT));
+    dim3 grid((nb + 31) / 32, P, nk);
+    k_reduce_proj<<<grid, dim3(32, 8), 0, st>>>(partial, W.splits, g1.part_rows, g1.part_ld, P, nb, W.HB,
+                                                static_cast<float2*>(projT));
     QGB_LAUNCH_CHECK("k_reduce_proj");
     dim3 grid2(1, static_cast<unsigned>(W.rowsB), nk);
     k_dapply_split<<<grid2, 256, 0, st>>>(static_cast<const float2*>(projT), static_cast<const float2*>(D),
@@ -627,7 +647,7 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
   g2.hc_ld = n_tot;
   g2.nb = nb;
   g2.err = err;
-  return launch<BN, (BN == 256 ? 4 : 6), EPI_ADD_HC>(
+  return launch<BN, kStages<BN>, EPI_ADD_HC>(
       Operand{t_hi, t_lo, n_tot, BL.ldT, static_cast<long long>(n_tot) * BL.ldT},
       Operand{b2_hi, b2_lo, W.rowsB, W.ldB2, W.rowsB * W.ldB2}, 2 * P, nk, g2, st);
 }

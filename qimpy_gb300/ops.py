@@ -181,8 +181,7 @@ def hamiltonian_mixed(sphere: DeviceSphere, C: torch.Tensor, split: torch.Tensor
         projT = torch.empty((C.shape[0], nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
         sptr, dptr, pptr = split.data_ptr(), D_blocks.data_ptr(), projT.data_ptr()
     if ws is None:
-        ws = workspace(int(_lib.lib().qgb_hamiltonian_mixed_workspace_bytes(ct.byref(sphere.struct), nb, P)),
-                       C.device)
+        ws = workspace(sphere.hamiltonian_mixed_workspace_bytes(nb, P), C.device)
     err = device_error_word(C.device)
     _lib.check(_lib.lib().qgb_hamiltonian_mixed(ct.byref(sphere.struct), C.data_ptr(), out.data_ptr(), nb, sptr,
                                                 dptr, n_atoms, pa, pptr, ws.data_ptr(), ws.numel(), err.data_ptr(),

@@ -180,11 +180,32 @@ class DeviceSphere:
         self._V = self.permute_real(V)
         self.struct.V = self._V.data_ptr()
 
-    def workspace_bytes(self, nb: int) -> int:
-        return int(_lib.lib().qgb_potential_workspace_bytes(ct.byref(self.struct), nb, self.qdtype))
+    #: Default bound on the slab planes of one band chunk: small enough that the
+    #: planes written by k_ifft_yz are still in L2 (126 MB) for k_xpass and
+    #: k_fft_yz_gather.  The autotuner may override it per sphere.
+    plane_budget_bytes = 1 << 30
+
+    def workspace_bytes(self, nb: int, budget: int | None = None) -> int:
+        """Workspace for `nb` bands, capped at the plane budget (the kernels then
+        process the bands in chunks that fit)."""
+        per_band = int(_lib.lib().qgb_potential_workspace_bytes(ct.byref(self.struct), 1, self.qdtype))
+        budget = self.plane_budget_bytes if budget is None else budget
+        chunk = max(1, min(nb, budget // max(per_band, 1)))
+        return per_band * chunk
 
     def hamiltonian_workspace_bytes(self, nb: int, P: int) -> int:
-        return int(_lib.lib().qgb_hamiltonian_workspace_bytes(ct.byref(self.struct), nb, P, self.qdtype))
+        """qgb_hamiltonian workspace: the nonlocal part plus capped slab planes."""
+        lib = _lib.lib()
+        full = int(lib.qgb_hamiltonian_workspace_bytes(ct.byref(self.struct), nb, P, self.qdtype))
+        planes = int(lib.qgb_potential_workspace_bytes(ct.byref(self.struct), nb, self.qdtype))
+        return full - planes + self.workspace_bytes(nb)
+
+    def hamiltonian_mixed_workspace_bytes(self, nb: int, P: int) -> int:
+        """qgb_hamiltonian_mixed workspace: tensor-core nonlocal part plus capped planes."""
+        lib = _lib.lib()
+        full = int(lib.qgb_hamiltonian_mixed_workspace_bytes(ct.byref(self.struct), nb, P))
+        planes = int(lib.qgb_potential_workspace_bytes(ct.byref(self.struct), nb, _lib.QGB_F32))
+        return full - planes + self.workspace_bytes(nb)
 
 
 def sphere_stats(t: SphereTables) -> dict:
