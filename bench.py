@@ -53,6 +53,7 @@ def parse_args():
     ap.add_argument("--eig-reps", type=int, default=3)
     ap.add_argument("--forms", default="fp64,mixed", help="precision forms to run (profiling aid)")
     ap.add_argument("--plane-budget-mb", type=int, default=0, help="slab-plane workspace cap (0 = default)")
+    ap.add_argument("--batch", type=int, default=256, help="instances of the batched workload (0 = skip)")
     ap.add_argument("--no-eigensolve", action="store_true")
     return ap.parse_args()
 
@@ -371,6 +372,72 @@ def run_eigensolves(args, local):
     return out
 
 
+def run_batch(args, local):
+    """Batched uneven instances: `args.batch` independent problems (cubic sides
+    10/14/18/22 bohr, 2-16 atoms, Ecut 15-25 Ha, 8-64 bands, 1-8 k-points),
+    FP32 H.psi with the tensor-core nonlocal term, FFT radix schedule per grid
+    from the autotuner, the whole batched H.psi captured in one CUDA graph and
+    replayed.  Reference point: the same instances applied one after another
+    with the single-problem C-ABI call (no batching, no graph)."""
+    import torch
+
+    from qimpy_gb300 import autotune, batch as bt, ops
+
+    dev = torch.device(f"cuda:{local}")
+    t0 = time.perf_counter()
+    specs = bt.make_batch_specs(count=args.batch)
+    shapes = sorted({(s.grid,) * 3 for s in specs})
+    sched = {sh: autotune.tune_shape(sh, torch.complex64, dev) for sh in shapes}
+    t_tune = time.perf_counter() - t0
+    insts = [bt.Instance(s, dev, fft_factors=sched[(s.grid,) * 3]) for s in specs]
+    bh = bt.BatchedHamiltonian(insts, dev)
+    bh.capture()
+    t_setup = time.perf_counter() - t0
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        bh.replay()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        bh.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    # Unbatched reference point: per-instance calls, eager.
+    ws = [ops.workspace(i.sphere.hamiltonian_mixed_workspace_bytes(i.nb, i.beta.shape[1]), dev) for i in insts]
+    outs = [torch.empty_like(i.C) for i in insts]
+
+    def sequential():
+        for i, w, o in zip(insts, ws, outs):
+            ops.hamiltonian_mixed(i.sphere, i.C, i.split, i.D, out=o, ws=w)
+
+    sequential()
+    torch.cuda.synchronize()
+    seq = []
+    for _ in range(max(1, args.steps // 2)):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sequential()
+        e1.record()
+        torch.cuda.synchronize()
+        seq.append(e0.elapsed_time(e1) * 1e-3)
+    agree = max(float((a - b).abs().max() / b.abs().max()) for a, b in zip(bh.outputs, outs))
+    n_sh = len(shapes)
+    return dict(instances=len(insts), band_apps_per_step=bh.band_apps, grids=f"{n_sh} shapes "
+                f"{shapes[0][0]}^3..{shapes[-1][0]}^3", value=bh.band_apps / float(np.median(times)),
+                unit=UNIT, ms_per_step=1e3 * float(np.median(times)),
+                sequential_value=bh.band_apps / float(np.median(seq)),
+                batched_over_sequential=float(np.median(seq)) / float(np.median(times)),
+                max_rel_diff_batched_vs_sequential=agree, launches_per_step=bh.launches(),
+                setup_s=t_setup, autotune_s=t_tune,
+                schedule={f"{k[0]}": [list(f) for f in v] for k, v in sched.items()},
+                error_word=int(ops.device_error_word(dev).item()))
+
+
 def cpu_baseline(args, p=None, b=None, beta=None, C=None, threads=None):
     """Oracle H.psi (FP64, numpy/scipy) on a bounded band sample, timed on host cores."""
     from oracle import hpsi as oh
@@ -447,6 +514,8 @@ def main():
     }
     if not args.no_eigensolve:
         out["eigensolve_si2"] = run_eigensolves(args, local)
+    if args.batch:
+        out["batch"] = run_batch(args, local)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:

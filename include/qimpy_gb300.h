@@ -87,6 +87,23 @@ typedef struct qgb_sphere {
   const void* V;            /* real of the call's dtype, permuted order */
 } qgb_sphere;
 
+/*
+ * One unit of a batched local-potential apply: a block of bands of one
+ * independent problem (its own cell, grid, k-points and basis).
+ *   sphere  DEVICE pointer to a copy of the problem's qgb_sphere
+ *   C, out  [nk][nb][n_tot] of that sphere (out may alias C)
+ *   planes  >= qgb_potential_workspace_bytes(sphere, nb, dtype) bytes, not
+ *           shared with any other item of the batch
+ */
+typedef struct qgb_batch_item {
+  const struct qgb_sphere* sphere;
+  const void* C;
+  void* out;
+  void* planes;
+  int32_t nb;
+  uint32_t flags;
+} qgb_batch_item;
+
 /* Library identification. */
 int qgb_abi_version(void);
 const char* qgb_last_error(void);
@@ -146,6 +163,24 @@ int qgb_apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out
 int qgb_apply_potential_static(const qgb_sphere* s, int dtype, const void* C, void* out, int nb,
                                unsigned flags, void* stream);
 size_t qgb_static_scratch_bytes(void);
+
+/*
+ * Shared memory per CTA the local-potential kernels need for a sphere (host).
+ */
+size_t qgb_sphere_smem_bytes(const qgb_sphere* s, int dtype);
+
+/*
+ * Batched Basis.apply_potential (qimpy/dft/electrons/_basis_ops.py:39-113) for
+ * many independent problems with uneven grids and bases: three launches (one
+ * per transform phase) for the whole batch.  `items` (device) lists the
+ * problems' band blocks; `slab_starts` and `row_starts` (device, n_items + 1
+ * prefix sums) give each item's work units: nk * nb * max_slabs for the y/z
+ * phases and nk * nb * N1 for the x phase; smem_bytes = max over items of
+ * qgb_sphere_smem_bytes.  Launch-only (capturable in a CUDA graph).
+ */
+int qgb_apply_potential_batched(const qgb_batch_item* items, int n_items, const long long* slab_starts,
+                                const long long* row_starts, long long n_slab_units, long long n_row_units,
+                                int dtype, size_t smem_bytes, void* stream);
 
 /*
  * projT[k][b][p] = sum_g conj(beta[k][p][g]) C[k][b][g]  (replaces Wavefunction.proj

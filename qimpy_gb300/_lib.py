@@ -34,6 +34,13 @@ class QgbSphere(ct.Structure):
     ]
 
 
+class QgbBatchItem(ct.Structure):
+    """Mirror of ``struct qgb_batch_item``."""
+
+    _fields_ = [("sphere", ct.c_void_p), ("C", ct.c_void_p), ("out", ct.c_void_p), ("planes", ct.c_void_p),
+                ("nb", ct.c_int32), ("flags", ct.c_uint32)]
+
+
 class QgbError(RuntimeError):
     """Nonzero status returned by the library."""
 
@@ -61,6 +68,9 @@ _SIGS = {
     "qgb_apply_potential_static": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
                                               ct.c_uint, ct.c_void_p]),
     "qgb_static_scratch_bytes": (ct.c_size_t, []),
+    "qgb_sphere_smem_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int]),
+    "qgb_apply_potential_batched": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_longlong,
+                                               ct.c_longlong, ct.c_int, ct.c_size_t, ct.c_void_p]),
     "qgb_beta_split_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int]),
     "qgb_beta_split": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
     "qgb_nonlocal_tc_workspace_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int, ct.c_int]),

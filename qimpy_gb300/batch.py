@@ -1,0 +1,251 @@
+"""Batched H.psi over many independent problems with uneven grids and bases.
+
+A batch holds independent problems ("instances": a cell with its own k-points,
+bands, cutoff and FFT grid), all resident on one GPU.  One batched H.psi runs
+the local potential of every instance's band block in three launches (one per
+transform phase, work units mapped to CTAs through prefix sums over the
+instances) and the tensor-core nonlocal term per instance; the whole
+application is captured once in a CUDA graph and replayed.
+
+Instance inputs (V(r), projectors, start vectors) are generated on the device
+from seeded specs, because the biggest cells have 100^3 grids.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib, ops
+from . import sphere as sp
+from . import workloads as wl
+
+CUBIC_SIDES = (10.0, 14.0, 18.0, 22.0)
+
+
+def reference_grid(L: float, ke_cutoff: float) -> int:
+    """Smallest codelet-factorable size >= the reference's minimum for a
+    wavefunction cutoff: L * 2 sqrt(2 Ecut) / pi rounded up to a multiple of 4
+    (qimpy/grid/_grid.py:114-127, density cutoff 4 Ecut)."""
+    n_min = int(4 * math.ceil(L * 2.0 * math.sqrt(2.0 * ke_cutoff) / math.pi / 4.0))
+    n = n_min
+    while True:
+        try:
+            sp.factor_axis(n)
+            return n
+        except ValueError:
+            n += 4
+
+
+@dataclass
+class InstanceSpec:
+    """One independent eigenproblem of a batch."""
+
+    index: int
+    side: float
+    positions: np.ndarray  # (n_atoms, 3) fractional
+    ke_cutoff: float
+    n_bands: int
+    k: np.ndarray  # (nk, 3)
+    seed: int
+    grid: int = 0
+
+    @property
+    def n_atoms(self) -> int:
+        return int(self.positions.shape[0])
+
+
+def make_batch_specs(count: int = 256, seed: int = 31, sides=CUBIC_SIDES, ke_range=(15.0, 25.0),
+                     atoms_range=(2, 16), bands_range=(8, 64), k_range=(1, 8)) -> list:
+    """Seeded instance specs: cubic side from `sides`, Gaussian-well atoms at
+    random positions, Ecut uniform in ke_range, bands and k-point counts
+    uniform in their ranges, k-points random in the Brillouin zone (so basis
+    sizes differ per k)."""
+    specs = []
+    u = wl.splitmix_uniform(seed, 500, count * 8)
+    for i in range(count):
+        r = u[8 * i : 8 * i + 8]
+        side = sides[int(r[0] * len(sides)) % len(sides)]
+        n_atoms = atoms_range[0] + int(r[1] * (atoms_range[1] - atoms_range[0] + 1))
+        ke = ke_range[0] + (ke_range[1] - ke_range[0]) * r[2]
+        nb = bands_range[0] + int(r[3] * (bands_range[1] - bands_range[0] + 1))
+        nk = k_range[0] + int(r[4] * (k_range[1] - k_range[0] + 1))
+        pos = wl.splitmix_uniform(seed, 1000 + i, 3 * n_atoms).reshape(n_atoms, 3)
+        kpts = wl.splitmix_uniform(seed, 5000 + i, 3 * nk).reshape(nk, 3) - 0.5
+        if nk == 1:
+            kpts[:] = 0.0
+        spec = InstanceSpec(i, side, pos, ke, nb, kpts, seed * 100003 + i)
+        spec.grid = reference_grid(side, ke)
+        specs.append(spec)
+    return specs
+
+
+class Instance:
+    """Device-resident data of one instance (mixed precision, complex64)."""
+
+    def __init__(self, spec: InstanceSpec, device, fft_factors=None, tune: bool = False):
+        self.spec = spec
+        dev = torch.device(device)
+        L, shape = spec.side, (spec.grid,) * 3
+        if fft_factors is None and tune:
+            from .autotune import tune_shape
+
+            fft_factors = tune_shape(shape, torch.complex64, dev)
+        R = np.eye(3) * L
+        Gb = 2.0 * np.pi * np.linalg.inv(R.T)
+        self.layout = wl.make_basis_device(Gb, spec.k, spec.ke_cutoff, shape, dev)
+        self.tables = sp.build_tables(self.layout.fft_index, self.layout.n, shape, fft_factors)
+        self.sphere = sp.DeviceSphere(self.tables, self.layout.ke, dev, torch.complex64)
+        self.nk, self.nb, self.n_tot = spec.k.shape[0], spec.n_bands, self.layout.n_tot
+        self.volume = L ** 3
+        g = torch.Generator(device=dev).manual_seed(spec.seed)
+        self.sphere.set_potential(self._potential(dev, g, L, shape))
+        self.beta, self.D = self._projectors(dev, Gb)
+        self.split = ops.beta_split(self.beta)
+        self.C = self._start_vectors(dev, g)
+
+    def _potential(self, dev, g, L, shape):
+        """Gaussian wells (depth 2 Ha, width 1.2 bohr, nearest image) plus
+        Fourier modes with amplitude ~ exp(-|G|^2/8), rms 0.3 Ha."""
+        N = shape[0]
+        x = torch.arange(N, device=dev, dtype=torch.float64) / N
+        X, Y, Z = torch.meshgrid(x, x, x, indexing="ij")
+        V = torch.zeros(shape, dtype=torch.float64, device=dev)
+        for tau in self.spec.positions:
+            d = [c - float(t) for c, t in zip((X, Y, Z), tau)]
+            d = [(t - torch.round(t)) * L for t in d]
+            V -= 2.0 * torch.exp(-(d[0] ** 2 + d[1] ** 2 + d[2] ** 2) / (2 * 1.2 ** 2))
+        iG = torch.fft.fftfreq(N, d=1.0 / N, device=dev, dtype=torch.float64) * (2 * math.pi / L)
+        G2 = iG[:, None, None] ** 2 + iG[None, :, None] ** 2 + iG[None, None, :] ** 2
+        c = torch.complex(torch.randn(shape, generator=g, device=dev, dtype=torch.float64),
+                          torch.randn(shape, generator=g, device=dev, dtype=torch.float64)) * torch.exp(-G2 / 8)
+        modes = torch.fft.ifftn(c, norm="forward").real
+        V += modes * (0.3 / modes.square().mean().sqrt())
+        return V
+
+    def _projectors(self, dev, Gb):
+        """s + p Gaussian projectors (sigma 1) on every atom, D = diag(1.5, -0.8 x3)."""
+        lay = self.layout
+        iG = torch.from_numpy(lay.iG).to(dev, torch.float64)
+        k = torch.from_numpy(self.spec.k).to(dev, torch.float64)
+        kiG = iG + k[:, None, :]
+        q = kiG @ torch.from_numpy(Gb.T).to(dev)
+        q2 = q.square().sum(-1)
+        rad = ((2 * math.pi) ** 1.5 * torch.exp(-0.5 * q2)).to(torch.complex128)
+        c1 = -1j * math.sqrt(3 / (4 * math.pi))
+        ang = torch.stack((torch.full_like(rad, 0.5 / math.sqrt(math.pi)),
+                           c1 * q[..., 1].to(torch.complex128),
+                           c1 * q[..., 2].to(torch.complex128),
+                           c1 * q[..., 0].to(torch.complex128)), dim=1) * rad[:, None, :]
+        pos = torch.from_numpy(self.spec.positions).to(dev, torch.float64)
+        phase = torch.exp(-2j * math.pi * torch.einsum("kgx,ax->kag", kiG, pos)) / math.sqrt(self.volume)
+        beta = (ang[:, None, :, :] * phase[:, :, None, :]).reshape(self.nk, -1, lay.n_tot)
+        mask = torch.arange(lay.n_tot, device=dev)[None, :] < torch.from_numpy(lay.n).to(dev)[:, None]
+        beta = (beta * mask[:, None, :]).to(torch.complex64).contiguous()
+        D = torch.diag(torch.tensor([1.5, -0.8, -0.8, -0.8], dtype=torch.complex64, device=dev))
+        return beta, D.expand(self.spec.n_atoms, 4, 4).contiguous()
+
+    def _start_vectors(self, dev, g):
+        ke = torch.from_numpy(self.layout.ke).to(dev)
+        mask = torch.arange(self.n_tot, device=dev)[None, :] < torch.from_numpy(self.layout.n).to(dev)[:, None]
+        C = torch.complex(torch.randn((self.nk, self.nb, self.n_tot), generator=g, device=dev),
+                          torch.randn((self.nk, self.nb, self.n_tot), generator=g, device=dev))
+        return (C / (1 + ke[:, None, :]) * mask[:, None, :]).to(torch.complex64).contiguous()
+
+    @property
+    def band_apps(self) -> int:
+        return self.nk * self.nb
+
+
+@dataclass
+class BatchedHamiltonian:
+    """H.psi for all instances of a batch in one graph-capturable sequence:
+    three batched local-potential launches for the whole batch, then the
+    tensor-core nonlocal term of each instance."""
+
+    instances: list
+    device: torch.device
+    inputs: list = field(default_factory=list)
+    outputs: list = field(default_factory=list)
+
+    def __post_init__(self):
+        lib = _lib.lib()
+        dev = self.device
+        n = len(self.instances)
+        # Device copies of every sphere descriptor.
+        ssz = ct.sizeof(_lib.QgbSphere)
+        host = bytearray(ssz * n)
+        for i, inst in enumerate(self.instances):
+            host[i * ssz : (i + 1) * ssz] = bytes(inst.sphere.struct)
+        self._spheres = torch.frombuffer(host, dtype=torch.uint8).to(dev)
+        # Inputs / outputs / plane workspaces.
+        self.inputs = [inst.C for inst in self.instances]
+        self.outputs = [torch.empty_like(inst.C) for inst in self.instances]
+        per = [inst.sphere.workspace_bytes(inst.nb, budget=1 << 62) for inst in self.instances]
+        offs = np.concatenate(([0], np.cumsum([(b + 255) // 256 * 256 for b in per])))
+        self._planes = torch.empty(int(offs[-1]), dtype=torch.uint8, device=dev)
+        items = (_lib.QgbBatchItem * n)()
+        slab_units, row_units = [0], [0]
+        smem = 0
+        for i, inst in enumerate(self.instances):
+            t = inst.tables
+            items[i].sphere = self._spheres.data_ptr() + i * ssz
+            items[i].C = self.inputs[i].data_ptr()
+            items[i].out = self.outputs[i].data_ptr()
+            items[i].planes = self._planes.data_ptr() + int(offs[i])
+            items[i].nb = inst.nb
+            items[i].flags = _lib.QGB_ADD_KE
+            slab_units.append(slab_units[-1] + t.nk * inst.nb * t.max_slabs)
+            row_units.append(row_units[-1] + t.nk * inst.nb * t.shape[1])
+            smem = max(smem, int(lib.qgb_sphere_smem_bytes(ct.byref(inst.sphere.struct), _lib.QGB_F32)))
+        self._items = torch.frombuffer(bytearray(bytes(items)), dtype=torch.uint8).to(dev)
+        self._slab_starts = torch.tensor(slab_units, dtype=torch.int64, device=dev)
+        self._row_starts = torch.tensor(row_units, dtype=torch.int64, device=dev)
+        self.n_slab_units, self.n_row_units, self.smem = slab_units[-1], row_units[-1], smem
+        self._nl_ws = [ops.workspace(int(lib.qgb_nonlocal_tc_workspace_bytes(inst.nk, inst.beta.shape[1], inst.nb,
+                                                                              inst.n_tot)), dev)
+                       for inst in self.instances]
+        self._projT = [torch.empty((inst.nk, inst.nb, inst.beta.shape[1]), dtype=torch.complex64, device=dev)
+                       for inst in self.instances]
+        self.graph = None
+
+    @property
+    def band_apps(self) -> int:
+        return sum(inst.band_apps for inst in self.instances)
+
+    def launches(self) -> int:
+        """Kernels of ours per application: 3 batched local + 5 per instance nonlocal."""
+        return 3 + 5 * len(self.instances)
+
+    def apply_local(self, stream=None):
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _lib.check(_lib.lib().qgb_apply_potential_batched(self._items.data_ptr(), len(self.instances),
+                                                           self._slab_starts.data_ptr(), self._row_starts.data_ptr(),
+                                                           self.n_slab_units, self.n_row_units, _lib.QGB_F32,
+                                                           self.smem, st), "apply_potential_batched")
+
+    def apply(self):
+        """Out_i = H_i C_i for every instance (inputs/outputs fixed at construction)."""
+        self.apply_local()
+        for i, inst in enumerate(self.instances):
+            ops.apply_nonlocal_tc(inst.split, inst.D, self.inputs[i], self.outputs[i], self._projT[i], self._nl_ws[i])
+
+    def capture(self):
+        """Capture apply() in a CUDA graph (after one eager warm-up call)."""
+        self.apply()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.apply()
+        torch.cuda.current_stream().wait_stream(s)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()

@@ -49,11 +49,10 @@ __device__ __forceinline__ size_t plane_index(const qgb_sphere& s, int k, int b,
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_ifft_yz(const qgb_sphere s, LocalParams lp,
-                                                      const cplx_t<T>* __restrict__ C,
-                                                      cplx_t<T>* __restrict__ planes) {
+__device__ __forceinline__ void body_ifft_yz(const qgb_sphere& s, const LocalParams& lp,
+                                             const cplx_t<T>* __restrict__ C, cplx_t<T>* __restrict__ planes,
+                                             const int slab, const int b, const int k) {
   using C2 = cplx_t<T>;
-  const int slab = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
   if (slab >= s.n_slabs[k]) return;
   const int N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
   const int lim = N1 * ld, Wy = lim, Wz = Wy + N1;  // shared layout: plane, W_y, W_z
@@ -95,10 +94,9 @@ __global__ void __launch_bounds__(kThreads) k_ifft_yz(const qgb_sphere s, LocalP
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalParams lp,
-                                                    cplx_t<T>* __restrict__ planes) {
+__device__ __forceinline__ void body_xpass(const qgb_sphere& s, const LocalParams& lp,
+                                           cplx_t<T>* __restrict__ planes, const int r1, const int b, const int k) {
   using C2 = cplx_t<T>;
-  const int r1 = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
   const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
   const int L1 = s.L1[0], L2 = s.L2[0];
   const int lim = N0 * ld, Wx = lim;  // shared layout: pencils (x rows of N2 columns), W_x
@@ -279,10 +277,10 @@ __device__ __forceinline__ void xmid_dispatch(int L1, cplx_t<T>* sm, int p, int 
 // step reads only shared memory.  Shared layout: pencils [N0][ldx = N2 + 2]
 // complex, W_x [N0] complex, V slice [N0][N2] real.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_xpass_async(const qgb_sphere s, LocalParams lp,
-                                                          cplx_t<T>* __restrict__ planes) {
+__device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const LocalParams& lp,
+                                                 cplx_t<T>* __restrict__ planes, const int r1, const int b,
+                                                 const int k) {
   using C2 = cplx_t<T>;
-  const int r1 = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
   const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 2;
   const int L1 = s.L1[0], L2 = s.L2[0];
   const int lim = N0 * ld, Wx = lim;
@@ -340,13 +338,11 @@ __global__ void __launch_bounds__(kThreads) k_xpass_async(const qgb_sphere s, Lo
   }
 }
 
-// C and out may alias (in-place apply): no __restrict__ on them.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, LocalParams lp,
-                                                            const cplx_t<T>* C, cplx_t<T>* out,
-                                                            const cplx_t<T>* __restrict__ planes) {
+__device__ __forceinline__ void body_fft_yz_gather(const qgb_sphere& s, const LocalParams& lp, const cplx_t<T>* C,
+                                                   cplx_t<T>* out, const cplx_t<T>* __restrict__ planes,
+                                                   const int slab, const int b, const int k) {
   using C2 = cplx_t<T>;
-  const int slab = blockIdx.x, b = blockIdx.y, k = blockIdx.z;
   const int nslabs = s.n_slabs[k];
   C2* Ob = out + (static_cast<size_t>(k) * lp.nb_total + lp.b0 + b) * s.n_tot;
   const bool accumulate = (lp.flags & QGB_ACCUMULATE) != 0;
@@ -400,6 +396,104 @@ __global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, 
     }
     Ob[g] = mk<T>(xr, xi);
   }
+}
+
+
+// ---------------------------------------------------------------------------
+// Kernels: one sphere (grid = work units of that sphere) ...
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_ifft_yz(const qgb_sphere s, LocalParams lp,
+                                                      const cplx_t<T>* __restrict__ C,
+                                                      cplx_t<T>* __restrict__ planes) {
+  body_ifft_yz<T>(s, lp, C, planes, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalParams lp,
+                                                    cplx_t<T>* __restrict__ planes) {
+  body_xpass<T>(s, lp, planes, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_xpass_async(const qgb_sphere s, LocalParams lp,
+                                                          cplx_t<T>* __restrict__ planes) {
+  body_xpass_async<T>(s, lp, planes, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// C and out may alias (in-place apply): no __restrict__ on them.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, LocalParams lp,
+                                                            const cplx_t<T>* C, cplx_t<T>* out,
+                                                            const cplx_t<T>* __restrict__ planes) {
+  body_fft_yz_gather<T>(s, lp, C, out, planes, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// ... and a batch of independent spheres (cells / k-point sets / band blocks
+// with their own grids and bases) in one launch per phase.  CTA u handles the
+// work unit u of the concatenated unit ranges starts[i] <= u < starts[i + 1]
+// of item i; units are (k, band, slab) for the y/z phases and (k, band, y-row)
+// for the x phase, in that order (slab / row fastest).
+
+__device__ __forceinline__ int batch_item_of(const long long* __restrict__ starts, int n_items, long long u) {
+  int lo = 0, hi = n_items - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(starts + mid) <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_ifft_yz_batched(const qgb_batch_item* __restrict__ items,
+                                                              const long long* __restrict__ starts, int n_items) {
+  const long long u = blockIdx.x;
+  const int i = batch_item_of(starts, n_items, u);
+  const qgb_batch_item it = items[i];
+  const qgb_sphere& s = *it.sphere;
+  const long long local = u - starts[i];
+  const int slab = static_cast<int>(local % s.max_slabs);
+  const long long rest = local / s.max_slabs;
+  const LocalParams lp{it.nb, 0, it.nb, it.flags};
+  body_ifft_yz<T>(s, lp, static_cast<const cplx_t<T>*>(it.C), static_cast<cplx_t<T>*>(it.planes), slab,
+                  static_cast<int>(rest % it.nb), static_cast<int>(rest / it.nb));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_xpass_batched(const qgb_batch_item* __restrict__ items,
+                                                            const long long* __restrict__ starts, int n_items) {
+  const long long u = blockIdx.x;
+  const int i = batch_item_of(starts, n_items, u);
+  const qgb_batch_item it = items[i];
+  const qgb_sphere& s = *it.sphere;
+  const long long local = u - starts[i];
+  const int r1 = static_cast<int>(local % s.N[1]);
+  const long long rest = local / s.N[1];
+  const LocalParams lp{it.nb, 0, it.nb, it.flags};
+  const int b = static_cast<int>(rest % it.nb), k = static_cast<int>(rest / it.nb);
+  if (sizeof(T) == 4 && s.N[2] % 4 == 0)
+    body_xpass_async<T>(s, lp, static_cast<cplx_t<T>*>(it.planes), r1, b, k);
+  else
+    body_xpass<T>(s, lp, static_cast<cplx_t<T>*>(it.planes), r1, b, k);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_fft_yz_gather_batched(const qgb_batch_item* __restrict__ items,
+                                                                    const long long* __restrict__ starts,
+                                                                    int n_items) {
+  const long long u = blockIdx.x;
+  const int i = batch_item_of(starts, n_items, u);
+  const qgb_batch_item it = items[i];
+  const qgb_sphere& s = *it.sphere;
+  const long long local = u - starts[i];
+  const int slab = static_cast<int>(local % s.max_slabs);
+  const long long rest = local / s.max_slabs;
+  const LocalParams lp{it.nb, 0, it.nb, it.flags};
+  body_fft_yz_gather<T>(s, lp, static_cast<const cplx_t<T>*>(it.C), static_cast<cplx_t<T>*>(it.out),
+                        static_cast<const cplx_t<T>*>(it.planes), slab, static_cast<int>(rest % it.nb),
+                        static_cast<int>(rest / it.nb));
 }
 
 template <typename T>
@@ -546,6 +640,46 @@ int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, in
     if (rc) return rc;
   }
   return QGB_OK;
+}
+
+size_t sphere_smem_bytes(const qgb_sphere& s, int dtype) {
+  size_t smem = plane_smem_bytes(s, dtype);
+  if (xpass_async_ok(s, dtype)) smem = std::max(smem, xpass_async_smem_bytes(s));
+  return smem;
+}
+
+template <typename T>
+static int launch_batched(const qgb_batch_item* items, int n_items, const long long* slab_starts,
+                          const long long* row_starts, long long n_slab, long long n_row, size_t smem,
+                          cudaStream_t st) {
+  static size_t configured = 0;
+  if (smem > configured) {
+    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_fft_yz_gather_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+    configured = smem;
+  }
+  k_ifft_yz_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_starts, n_items);
+  QGB_LAUNCH_CHECK("k_ifft_yz_batched");
+  k_xpass_batched<T><<<static_cast<unsigned>(n_row), kThreads, smem, st>>>(items, row_starts, n_items);
+  QGB_LAUNCH_CHECK("k_xpass_batched");
+  k_fft_yz_gather_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_starts, n_items);
+  QGB_LAUNCH_CHECK("k_fft_yz_gather_batched");
+  return QGB_OK;
+}
+
+int apply_potential_batched(const qgb_batch_item* items, int n_items, const long long* slab_starts,
+                            const long long* row_starts, long long n_slab, long long n_row, int dtype, size_t smem,
+                            cudaStream_t st) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
+  if (n_items < 0 || n_slab < 0 || n_row < 0) return fail(QGB_ERR_INVALID, "negative batch sizes");
+  if (n_items == 0 || n_slab == 0) return QGB_OK;
+  if (!items || !slab_starts || !row_starts) return fail(QGB_ERR_INVALID, "NULL batch table");
+  if (n_slab > 0x7FFFFFFFLL || n_row > 0x7FFFFFFFLL) return fail(QGB_ERR_UNSUPPORTED, "batch too large for one grid");
+  if (smem > 227 * 1024) return fail(QGB_ERR_UNSUPPORTED, "batched shared memory %zu B > 227 KB", smem);
+  return dtype == QGB_F64 ? launch_batched<double>(items, n_items, slab_starts, row_starts, n_slab, n_row, smem, st)
+                          : launch_batched<float>(items, n_items, slab_starts, row_starts, n_slab, n_row, smem, st);
 }
 
 int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, cudaStream_t st) {

@@ -167,6 +167,25 @@ class DeviceSphere:
     def shape(self) -> tuple:
         return self.tables.shape
 
+    def set_factors(self, fac) -> None:
+        """Change the per-axis FFT factorisation (L1, L2): new twiddles, new
+        real-space permutation, potential re-permuted.  Sphere tables unchanged."""
+        fac = tuple(factor_axis(self.shape[a], tuple(fac[a])) for a in range(3))
+        V_real = None
+        if self._V is not None:  # undo the old permutation
+            inv = [np.argsort(p) for p in self.perms]
+            p0, p1, p2 = (torch.from_numpy(i).to(self._V.device) for i in inv)
+            V_real = self._V[p0][:, p1][:, :, p2]
+        self.tables.fac = fac
+        tw = np.concatenate([twiddle_table(self.shape[a], *fac[a]) for a in range(3)])
+        self._tw = torch.from_numpy(tw).to(self.cdtype).to(self.device)
+        self.perms = [permutation(self.shape[a], *fac[a]) for a in range(3)]
+        for a in range(3):
+            self.struct.L1[a], self.struct.L2[a] = fac[a]
+        self.struct.twiddle = self._tw.data_ptr()
+        if V_real is not None:
+            self.set_potential(V_real)
+
     def permute_real(self, V_r: torch.Tensor) -> torch.Tensor:
         """V in the kernels' digit-permuted real-space order (a gather on device)."""
         p0, p1, p2 = (torch.from_numpy(p).to(V_r.device) for p in self.perms)

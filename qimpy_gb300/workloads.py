@@ -220,6 +220,34 @@ def make_basis(Gbasis: np.ndarray, k: np.ndarray, ke_cutoff: float, shape) -> Ba
     return BasisLayout(tuple(shape), n.astype(np.int64), n_tot, fft_index.astype(np.int64), iG, ke)
 
 
+def make_basis_device(Gbasis: np.ndarray, k: np.ndarray, ke_cutoff: float, shape, device="cuda") -> BasisLayout:
+    """`make_basis` evaluated with torch on a device (for large grids).
+
+    Same ordering rule without the sort: in-sphere points in ascending linear
+    index, then the first out-of-sphere points as padding up to n_tot."""
+    import torch
+
+    dev = torch.device(device)
+    iG_grid = torch.from_numpy(grid_iG(shape)).to(dev)
+    Gb = torch.from_numpy(np.ascontiguousarray(Gbasis.T)).to(dev)
+    kt = torch.from_numpy(np.asarray(k, dtype=np.float64)).to(dev)
+    within = []
+    for ik in range(kt.shape[0]):
+        G = (iG_grid.to(torch.float64) + kt[ik]) @ Gb
+        within.append(0.5 * G.square().sum(dim=1) < ke_cutoff)
+    n = torch.stack([w.sum() for w in within]).cpu().numpy().astype(np.int64)
+    n_tot = int(n.max())
+    fft_index = torch.empty((len(within), n_tot), dtype=torch.int64, device=dev)
+    for ik, w in enumerate(within):
+        inside = torch.nonzero(w).flatten()
+        outside = torch.nonzero(~w).flatten()[: n_tot - inside.numel()]
+        fft_index[ik] = torch.cat((inside, outside))
+    iG = iG_grid[fft_index]
+    Gk = (iG.to(torch.float64) + kt[:, None, :]) @ Gb
+    ke = 0.5 * Gk.square().sum(dim=-1)
+    return BasisLayout(tuple(shape), n, n_tot, fft_index.cpu().numpy(), iG.cpu().numpy(), ke.cpu().numpy())
+
+
 # ---------------------------------------------------------------------------
 # Field and projector generators
 # ---------------------------------------------------------------------------
