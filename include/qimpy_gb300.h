@@ -175,12 +175,14 @@ size_t qgb_sphere_smem_bytes(const qgb_sphere* s, int dtype);
  * per transform phase) for the whole batch.  `items` (device) lists the
  * problems' band blocks; `slab_starts` and `row_starts` (device, n_items + 1
  * prefix sums) give each item's work units: nk * nb * max_slabs for the y/z
- * phases and nk * nb * N1 for the x phase; smem_bytes = max over items of
- * qgb_sphere_smem_bytes.  Launch-only (capturable in a CUDA graph).
+ * phases and nk * nb * N1 for the x phase; `slab_item` / `row_item` (device,
+ * one int per unit) name the item of every unit; smem_bytes = max over items
+ * of qgb_sphere_smem_bytes.  Launch-only (capturable in a CUDA graph).
  */
-int qgb_apply_potential_batched(const qgb_batch_item* items, int n_items, const long long* slab_starts,
-                                const long long* row_starts, long long n_slab_units, long long n_row_units,
-                                int dtype, size_t smem_bytes, void* stream);
+int qgb_apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,
+                                const long long* slab_starts, const int* row_item, const long long* row_starts,
+                                long long n_slab_units, long long n_row_units, int dtype, size_t smem_bytes,
+                                void* stream);
 
 /*
  * projT[k][b][p] = sum_g conj(beta[k][p][g]) C[k][b][g]  (replaces Wavefunction.proj

@@ -160,11 +160,66 @@ class Instance:
         return self.nk * self.nb
 
 
+class _Group:
+    """Instances sharing one grid shape: one batched launch per transform phase,
+    with that shape's shared-memory size."""
+
+    def __init__(self, instances: list, inputs: list, outputs: list, device):
+        lib = _lib.lib()
+        self.instances, self.inputs, self.outputs = instances, inputs, outputs
+        n = len(instances)
+        ssz = ct.sizeof(_lib.QgbSphere)
+        host = bytearray(ssz * n)
+        for i, inst in enumerate(instances):
+            host[i * ssz : (i + 1) * ssz] = bytes(inst.sphere.struct)
+        self._spheres = torch.frombuffer(host, dtype=torch.uint8).to(device)
+        per = [inst.sphere.workspace_bytes(inst.nb, budget=1 << 62) for inst in instances]
+        offs = np.concatenate(([0], np.cumsum([(b + 255) // 256 * 256 for b in per])))
+        self._planes = torch.empty(int(offs[-1]), dtype=torch.uint8, device=device)
+        items = (_lib.QgbBatchItem * n)()
+        slab_units, row_units, smem = [0], [0], 0
+        for i, inst in enumerate(instances):
+            t = inst.tables
+            items[i].sphere = self._spheres.data_ptr() + i * ssz
+            items[i].C = inputs[i].data_ptr()
+            items[i].out = outputs[i].data_ptr()
+            items[i].planes = self._planes.data_ptr() + int(offs[i])
+            items[i].nb = inst.nb
+            items[i].flags = _lib.QGB_ADD_KE
+            slab_units.append(slab_units[-1] + t.nk * inst.nb * t.max_slabs)
+            row_units.append(row_units[-1] + t.nk * inst.nb * t.shape[1])
+            smem = max(smem, int(lib.qgb_sphere_smem_bytes(ct.byref(inst.sphere.struct), _lib.QGB_F32)))
+        self._items = torch.frombuffer(bytearray(bytes(items)), dtype=torch.uint8).to(device)
+        self._slab_starts = torch.tensor(slab_units, dtype=torch.int64, device=device)
+        self._row_starts = torch.tensor(row_units, dtype=torch.int64, device=device)
+        ids = np.arange(n, dtype=np.int32)
+        self._slab_item = torch.from_numpy(np.repeat(ids, np.diff(slab_units))).to(device)
+        self._row_item = torch.from_numpy(np.repeat(ids, np.diff(row_units))).to(device)
+        self.n_slab_units, self.n_row_units, self.smem = slab_units[-1], row_units[-1], smem
+        self._nl_ws = [ops.workspace(int(lib.qgb_nonlocal_tc_workspace_bytes(i.nk, i.beta.shape[1], i.nb, i.n_tot)),
+                                     device) for i in instances]
+        self._projT = [torch.empty((i.nk, i.nb, i.beta.shape[1]), dtype=torch.complex64, device=device)
+                       for i in instances]
+
+    def apply(self):
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(_lib.lib().qgb_apply_potential_batched(self._items.data_ptr(), len(self.instances),
+                                                           self._slab_item.data_ptr(), self._slab_starts.data_ptr(),
+                                                           self._row_item.data_ptr(), self._row_starts.data_ptr(),
+                                                           self.n_slab_units, self.n_row_units, _lib.QGB_F32,
+                                                           self.smem, st), "apply_potential_batched")
+        for i, inst in enumerate(self.instances):
+            ops.apply_nonlocal_tc(inst.split, inst.D, self.inputs[i], self.outputs[i], self._projT[i], self._nl_ws[i])
+
+
 @dataclass
 class BatchedHamiltonian:
-    """H.psi for all instances of a batch in one graph-capturable sequence:
-    three batched local-potential launches for the whole batch, then the
-    tensor-core nonlocal term of each instance."""
+    """H.psi for all instances of a batch in one graph-capturable sequence.
+
+    Instances are grouped by FFT grid shape; each group runs its local
+    potential in three batched launches (shared memory sized for that shape)
+    followed by the tensor-core nonlocal term of its instances.  Groups run on
+    separate streams, so a captured graph has one parallel branch per group."""
 
     instances: list
     device: torch.device
@@ -172,44 +227,17 @@ class BatchedHamiltonian:
     outputs: list = field(default_factory=list)
 
     def __post_init__(self):
-        lib = _lib.lib()
         dev = self.device
-        n = len(self.instances)
-        # Device copies of every sphere descriptor.
-        ssz = ct.sizeof(_lib.QgbSphere)
-        host = bytearray(ssz * n)
-        for i, inst in enumerate(self.instances):
-            host[i * ssz : (i + 1) * ssz] = bytes(inst.sphere.struct)
-        self._spheres = torch.frombuffer(host, dtype=torch.uint8).to(dev)
-        # Inputs / outputs / plane workspaces.
         self.inputs = [inst.C for inst in self.instances]
         self.outputs = [torch.empty_like(inst.C) for inst in self.instances]
-        per = [inst.sphere.workspace_bytes(inst.nb, budget=1 << 62) for inst in self.instances]
-        offs = np.concatenate(([0], np.cumsum([(b + 255) // 256 * 256 for b in per])))
-        self._planes = torch.empty(int(offs[-1]), dtype=torch.uint8, device=dev)
-        items = (_lib.QgbBatchItem * n)()
-        slab_units, row_units = [0], [0]
-        smem = 0
+        by_shape: dict = {}
         for i, inst in enumerate(self.instances):
-            t = inst.tables
-            items[i].sphere = self._spheres.data_ptr() + i * ssz
-            items[i].C = self.inputs[i].data_ptr()
-            items[i].out = self.outputs[i].data_ptr()
-            items[i].planes = self._planes.data_ptr() + int(offs[i])
-            items[i].nb = inst.nb
-            items[i].flags = _lib.QGB_ADD_KE
-            slab_units.append(slab_units[-1] + t.nk * inst.nb * t.max_slabs)
-            row_units.append(row_units[-1] + t.nk * inst.nb * t.shape[1])
-            smem = max(smem, int(lib.qgb_sphere_smem_bytes(ct.byref(inst.sphere.struct), _lib.QGB_F32)))
-        self._items = torch.frombuffer(bytearray(bytes(items)), dtype=torch.uint8).to(dev)
-        self._slab_starts = torch.tensor(slab_units, dtype=torch.int64, device=dev)
-        self._row_starts = torch.tensor(row_units, dtype=torch.int64, device=dev)
-        self.n_slab_units, self.n_row_units, self.smem = slab_units[-1], row_units[-1], smem
-        self._nl_ws = [ops.workspace(int(lib.qgb_nonlocal_tc_workspace_bytes(inst.nk, inst.beta.shape[1], inst.nb,
-                                                                              inst.n_tot)), dev)
-                       for inst in self.instances]
-        self._projT = [torch.empty((inst.nk, inst.nb, inst.beta.shape[1]), dtype=torch.complex64, device=dev)
-                       for inst in self.instances]
+            by_shape.setdefault(inst.tables.shape, []).append(i)
+        # Largest groups first: their branches start earliest.
+        order = sorted(by_shape.values(), key=lambda idx: -sum(self.instances[i].band_apps for i in idx))
+        self.groups = [_Group([self.instances[i] for i in idx], [self.inputs[i] for i in idx],
+                              [self.outputs[i] for i in idx], dev) for idx in order]
+        self._streams = [torch.cuda.Stream(device=dev) for _ in self.groups]
         self.graph = None
 
     @property
@@ -217,33 +245,30 @@ class BatchedHamiltonian:
         return sum(inst.band_apps for inst in self.instances)
 
     def launches(self) -> int:
-        """Kernels of ours per application: 3 batched local + 5 per instance nonlocal."""
-        return 3 + 5 * len(self.instances)
-
-    def apply_local(self, stream=None):
-        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        _lib.check(_lib.lib().qgb_apply_potential_batched(self._items.data_ptr(), len(self.instances),
-                                                           self._slab_starts.data_ptr(), self._row_starts.data_ptr(),
-                                                           self.n_slab_units, self.n_row_units, _lib.QGB_F32,
-                                                           self.smem, st), "apply_potential_batched")
+        """Kernels of ours per application: 3 batched local per group + 5 per instance nonlocal."""
+        return 3 * len(self.groups) + 5 * len(self.instances)
 
     def apply(self):
         """Out_i = H_i C_i for every instance (inputs/outputs fixed at construction)."""
-        self.apply_local()
-        for i, inst in enumerate(self.instances):
-            ops.apply_nonlocal_tc(inst.split, inst.D, self.inputs[i], self.outputs[i], self._projT[i], self._nl_ws[i])
+        main = torch.cuda.current_stream()
+        for g, s in zip(self.groups, self._streams):
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                g.apply()
+        for s in self._streams:
+            main.wait_stream(s)
 
     def capture(self):
         """Capture apply() in a CUDA graph (after one eager warm-up call)."""
         self.apply()
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
-        s = torch.cuda.Stream()
-        s.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(s):
-            with torch.cuda.graph(g, stream=s):
+        cap = torch.cuda.Stream(device=self.device)
+        cap.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g, stream=cap):
                 self.apply()
-        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.current_stream().wait_stream(cap)
         self.graph = g
         return g
 

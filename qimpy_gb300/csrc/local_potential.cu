@@ -433,67 +433,73 @@ __global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, 
 // ... and a batch of independent spheres (cells / k-point sets / band blocks
 // with their own grids and bases) in one launch per phase.  CTA u handles the
 // work unit u of the concatenated unit ranges starts[i] <= u < starts[i + 1]
-// of item i; units are (k, band, slab) for the y/z phases and (k, band, y-row)
-// for the x phase, in that order (slab / row fastest).
+// of item i = unit_item[u]; units are (k, band, slab) for the y/z phases and
+// (k, band, y-row) for the x phase, in that order (slab / row fastest).  The
+// item and its sphere descriptor are staged in shared memory once per CTA.
 
-__device__ __forceinline__ int batch_item_of(const long long* __restrict__ starts, int n_items, long long u) {
-  int lo = 0, hi = n_items - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(starts + mid) <= u) lo = mid;
-    else hi = mid - 1;
+struct BatchCtx {
+  qgb_batch_item it;
+  qgb_sphere s;
+  long long local;
+};
+
+__device__ __forceinline__ void load_batch_ctx(BatchCtx& ctx, const qgb_batch_item* __restrict__ items,
+                                               const int* __restrict__ unit_item,
+                                               const long long* __restrict__ starts) {
+  if (threadIdx.x == 0) {
+    const long long u = blockIdx.x;
+    const int i = __ldg(unit_item + u);
+    ctx.it = items[i];
+    ctx.s = *ctx.it.sphere;
+    ctx.local = u - __ldg(starts + i);
   }
-  return lo;
+  __syncthreads();
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_ifft_yz_batched(const qgb_batch_item* __restrict__ items,
-                                                              const long long* __restrict__ starts, int n_items) {
-  const long long u = blockIdx.x;
-  const int i = batch_item_of(starts, n_items, u);
-  const qgb_batch_item it = items[i];
-  const qgb_sphere& s = *it.sphere;
-  const long long local = u - starts[i];
-  const int slab = static_cast<int>(local % s.max_slabs);
-  const long long rest = local / s.max_slabs;
-  const LocalParams lp{it.nb, 0, it.nb, it.flags};
-  body_ifft_yz<T>(s, lp, static_cast<const cplx_t<T>*>(it.C), static_cast<cplx_t<T>*>(it.planes), slab,
-                  static_cast<int>(rest % it.nb), static_cast<int>(rest / it.nb));
+                                                              const int* __restrict__ unit_item,
+                                                              const long long* __restrict__ starts) {
+  __shared__ BatchCtx ctx;
+  load_batch_ctx(ctx, items, unit_item, starts);
+  const qgb_sphere& s = ctx.s;
+  const int slab = static_cast<int>(ctx.local % s.max_slabs);
+  const long long rest = ctx.local / s.max_slabs;
+  const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
+  body_ifft_yz<T>(s, lp, static_cast<const cplx_t<T>*>(ctx.it.C), static_cast<cplx_t<T>*>(ctx.it.planes), slab,
+                  static_cast<int>(rest % ctx.it.nb), static_cast<int>(rest / ctx.it.nb));
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_xpass_batched(const qgb_batch_item* __restrict__ items,
-                                                            const long long* __restrict__ starts, int n_items) {
-  const long long u = blockIdx.x;
-  const int i = batch_item_of(starts, n_items, u);
-  const qgb_batch_item it = items[i];
-  const qgb_sphere& s = *it.sphere;
-  const long long local = u - starts[i];
-  const int r1 = static_cast<int>(local % s.N[1]);
-  const long long rest = local / s.N[1];
-  const LocalParams lp{it.nb, 0, it.nb, it.flags};
-  const int b = static_cast<int>(rest % it.nb), k = static_cast<int>(rest / it.nb);
+                                                            const int* __restrict__ unit_item,
+                                                            const long long* __restrict__ starts) {
+  __shared__ BatchCtx ctx;
+  load_batch_ctx(ctx, items, unit_item, starts);
+  const qgb_sphere& s = ctx.s;
+  const int r1 = static_cast<int>(ctx.local % s.N[1]);
+  const long long rest = ctx.local / s.N[1];
+  const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
+  const int b = static_cast<int>(rest % ctx.it.nb), k = static_cast<int>(rest / ctx.it.nb);
   if (sizeof(T) == 4 && s.N[2] % 4 == 0)
-    body_xpass_async<T>(s, lp, static_cast<cplx_t<T>*>(it.planes), r1, b, k);
+    body_xpass_async<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k);
   else
-    body_xpass<T>(s, lp, static_cast<cplx_t<T>*>(it.planes), r1, b, k);
+    body_xpass<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_fft_yz_gather_batched(const qgb_batch_item* __restrict__ items,
-                                                                    const long long* __restrict__ starts,
-                                                                    int n_items) {
-  const long long u = blockIdx.x;
-  const int i = batch_item_of(starts, n_items, u);
-  const qgb_batch_item it = items[i];
-  const qgb_sphere& s = *it.sphere;
-  const long long local = u - starts[i];
-  const int slab = static_cast<int>(local % s.max_slabs);
-  const long long rest = local / s.max_slabs;
-  const LocalParams lp{it.nb, 0, it.nb, it.flags};
-  body_fft_yz_gather<T>(s, lp, static_cast<const cplx_t<T>*>(it.C), static_cast<cplx_t<T>*>(it.out),
-                        static_cast<const cplx_t<T>*>(it.planes), slab, static_cast<int>(rest % it.nb),
-                        static_cast<int>(rest / it.nb));
+                                                                    const int* __restrict__ unit_item,
+                                                                    const long long* __restrict__ starts) {
+  __shared__ BatchCtx ctx;
+  load_batch_ctx(ctx, items, unit_item, starts);
+  const qgb_sphere& s = ctx.s;
+  const int slab = static_cast<int>(ctx.local % s.max_slabs);
+  const long long rest = ctx.local / s.max_slabs;
+  const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
+  body_fft_yz_gather<T>(s, lp, static_cast<const cplx_t<T>*>(ctx.it.C), static_cast<cplx_t<T>*>(ctx.it.out),
+                        static_cast<const cplx_t<T>*>(ctx.it.planes), slab, static_cast<int>(rest % ctx.it.nb),
+                        static_cast<int>(rest / ctx.it.nb));
 }
 
 template <typename T>
@@ -649,9 +655,9 @@ size_t sphere_smem_bytes(const qgb_sphere& s, int dtype) {
 }
 
 template <typename T>
-static int launch_batched(const qgb_batch_item* items, int n_items, const long long* slab_starts,
-                          const long long* row_starts, long long n_slab, long long n_row, size_t smem,
-                          cudaStream_t st) {
+static int launch_batched(const qgb_batch_item* items, const int* slab_item, const long long* slab_starts,
+                          const int* row_item, const long long* row_starts, long long n_slab, long long n_row,
+                          size_t smem, cudaStream_t st) {
   static size_t configured = 0;
   if (smem > configured) {
     QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -660,26 +666,27 @@ static int launch_batched(const qgb_batch_item* items, int n_items, const long l
                                         (int)smem));
     configured = smem;
   }
-  k_ifft_yz_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_starts, n_items);
+  k_ifft_yz_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_item, slab_starts);
   QGB_LAUNCH_CHECK("k_ifft_yz_batched");
-  k_xpass_batched<T><<<static_cast<unsigned>(n_row), kThreads, smem, st>>>(items, row_starts, n_items);
+  k_xpass_batched<T><<<static_cast<unsigned>(n_row), kThreads, smem, st>>>(items, row_item, row_starts);
   QGB_LAUNCH_CHECK("k_xpass_batched");
-  k_fft_yz_gather_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_starts, n_items);
+  k_fft_yz_gather_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_item, slab_starts);
   QGB_LAUNCH_CHECK("k_fft_yz_gather_batched");
   return QGB_OK;
 }
 
-int apply_potential_batched(const qgb_batch_item* items, int n_items, const long long* slab_starts,
-                            const long long* row_starts, long long n_slab, long long n_row, int dtype, size_t smem,
-                            cudaStream_t st) {
+int apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,
+                            const long long* slab_starts, const int* row_item, const long long* row_starts,
+                            long long n_slab, long long n_row, int dtype, size_t smem, cudaStream_t st) {
   if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
   if (n_items < 0 || n_slab < 0 || n_row < 0) return fail(QGB_ERR_INVALID, "negative batch sizes");
   if (n_items == 0 || n_slab == 0) return QGB_OK;
-  if (!items || !slab_starts || !row_starts) return fail(QGB_ERR_INVALID, "NULL batch table");
+  if (!items || !slab_starts || !row_starts || !slab_item || !row_item) return fail(QGB_ERR_INVALID, "NULL batch table");
   if (n_slab > 0x7FFFFFFFLL || n_row > 0x7FFFFFFFLL) return fail(QGB_ERR_UNSUPPORTED, "batch too large for one grid");
   if (smem > 227 * 1024) return fail(QGB_ERR_UNSUPPORTED, "batched shared memory %zu B > 227 KB", smem);
-  return dtype == QGB_F64 ? launch_batched<double>(items, n_items, slab_starts, row_starts, n_slab, n_row, smem, st)
-                          : launch_batched<float>(items, n_items, slab_starts, row_starts, n_slab, n_row, smem, st);
+  return dtype == QGB_F64
+             ? launch_batched<double>(items, slab_item, slab_starts, row_item, row_starts, n_slab, n_row, smem, st)
+             : launch_batched<float>(items, slab_item, slab_starts, row_item, row_starts, n_slab, n_row, smem, st);
 }
 
 int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, cudaStream_t st) {
