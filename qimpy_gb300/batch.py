@@ -84,9 +84,10 @@ def make_batch_specs(count: int = 256, seed: int = 31, sides=CUBIC_SIDES, ke_ran
 
 
 class Instance:
-    """Device-resident data of one instance (mixed precision, complex64)."""
+    """Device-resident data of one instance (complex64 by default)."""
 
-    def __init__(self, spec: InstanceSpec, device, fft_factors=None, tune: bool = False):
+    def __init__(self, spec: InstanceSpec, device, fft_factors=None, tune: bool = False,
+                 dtype: torch.dtype = torch.complex64):
         self.spec = spec
         dev = torch.device(device)
         L, shape = spec.side, (spec.grid,) * 3
@@ -98,13 +99,16 @@ class Instance:
         Gb = 2.0 * np.pi * np.linalg.inv(R.T)
         self.layout = wl.make_basis_device(Gb, spec.k, spec.ke_cutoff, shape, dev)
         self.tables = sp.build_tables(self.layout.fft_index, self.layout.n, shape, fft_factors)
-        self.sphere = sp.DeviceSphere(self.tables, self.layout.ke, dev, torch.complex64)
+        self.dtype = dtype
+        self.sphere = sp.DeviceSphere(self.tables, self.layout.ke, dev, dtype)
+        self.Rbasis, self.fft_factors = R, self.tables.fac
         self.nk, self.nb, self.n_tot = spec.k.shape[0], spec.n_bands, self.layout.n_tot
         self.volume = L ** 3
         g = torch.Generator(device=dev).manual_seed(spec.seed)
-        self.sphere.set_potential(self._potential(dev, g, L, shape))
+        self.V_r = self._potential(dev, g, L, shape)
+        self.sphere.set_potential(self.V_r)
         self.beta, self.D = self._projectors(dev, Gb)
-        self.split = ops.beta_split(self.beta)
+        self.split = ops.beta_split(self.beta) if dtype == torch.complex64 else None
         self.C = self._start_vectors(dev, g)
 
     def _potential(self, dev, g, L, shape):
@@ -144,8 +148,8 @@ class Instance:
         phase = torch.exp(-2j * math.pi * torch.einsum("kgx,ax->kag", kiG, pos)) / math.sqrt(self.volume)
         beta = (ang[:, None, :, :] * phase[:, :, None, :]).reshape(self.nk, -1, lay.n_tot)
         mask = torch.arange(lay.n_tot, device=dev)[None, :] < torch.from_numpy(lay.n).to(dev)[:, None]
-        beta = (beta * mask[:, None, :]).to(torch.complex64).contiguous()
-        D = torch.diag(torch.tensor([1.5, -0.8, -0.8, -0.8], dtype=torch.complex64, device=dev))
+        beta = (beta * mask[:, None, :]).to(self.dtype).contiguous()
+        D = torch.diag(torch.tensor([1.5, -0.8, -0.8, -0.8], dtype=self.dtype, device=dev))
         return beta, D.expand(self.spec.n_atoms, 4, 4).contiguous()
 
     def _start_vectors(self, dev, g):
@@ -153,7 +157,48 @@ class Instance:
         mask = torch.arange(self.n_tot, device=dev)[None, :] < torch.from_numpy(self.layout.n).to(dev)[:, None]
         C = torch.complex(torch.randn((self.nk, self.nb, self.n_tot), generator=g, device=dev),
                           torch.randn((self.nk, self.nb, self.n_tot), generator=g, device=dev))
-        return (C / (1 + ke[:, None, :]) * mask[:, None, :]).to(torch.complex64).contiguous()
+        return (C / (1 + ke[:, None, :]) * mask[:, None, :]).to(self.dtype).contiguous()
+
+    def electrons(self, n_bands: int):
+        """Electrons (mirror API) of this instance for an eigensolve of the lowest
+        `n_bands` bands (n_bands_extra = max(1, ceil(0.1 n_bands)), the
+        reference's default, qimpy/dft/electrons/_fillings.py:236-243), sharing
+        this instance's device data; start vectors orthonormalised."""
+        from . import electrons as E
+
+        spec = self.spec
+        basis = E.Basis.__new__(E.Basis)
+        basis.Rbasis, basis.Gbasis = self.Rbasis, 2.0 * np.pi * np.linalg.inv(self.Rbasis.T)
+        basis.volume, basis.k, basis.wk = self.volume, spec.k, np.full(len(spec.k), 1.0 / len(spec.k))
+        basis.ke_cutoff, basis.grid_shape, basis.device, basis.dtype = spec.ke_cutoff, self.tables.shape, \
+            self.sphere.device, self.dtype
+        basis.layout, basis.n, basis.n_tot = self.layout, self.layout.n, self.layout.n_tot
+        basis.n_min, basis.n_max = int(self.layout.n.min()), int(self.layout.n.max())
+        basis.fft_index, basis.iG, basis.tables, basis.sphere = self.layout.fft_index, self.layout.iG, \
+            self.tables, self.sphere
+        basis.ke = torch.from_numpy(self.layout.ke).to(self.sphere.device)
+        pad = torch.arange(basis.n_tot)[None, :] < torch.from_numpy(basis.n)[:, None]
+        basis.mask = pad.to(self.sphere.device)
+        basis._V_id = id(self.V_r)
+        ions = E.Ions.__new__(E.Ions)
+        ions.basis, ions.beta, ions.D = basis, self.beta, self.D
+        ions.n_projectors, ions.beta_split, ions.beta_version = int(self.beta.shape[1]), self.split, 0
+        extra = max(1, int(math.ceil(0.1 * n_bands)))
+        el = E.Electrons.__new__(E.Electrons)
+        el.basis, el.ions, el.V_r = basis, ions, self.V_r
+        el.n_bands, el.n_bands_extra = n_bands, extra
+        el.eig, el.deig_max, el.hpsi_band_count = None, np.inf, 0
+        C = self.C[:, : n_bands + extra]
+        if C.shape[1] < n_bands + extra:  # more bands requested than generated: extend deterministically
+            g = torch.Generator(device=self.sphere.device).manual_seed(spec.seed + 7)
+            more = torch.complex(torch.randn((self.nk, n_bands + extra - C.shape[1], self.n_tot), generator=g,
+                                             device=self.sphere.device),
+                                 torch.randn((self.nk, n_bands + extra - C.shape[1], self.n_tot), generator=g,
+                                             device=self.sphere.device)).to(self.dtype)
+            more = more / (1 + basis.ke[:, None, :]) * basis.mask[:, None, :]
+            C = torch.cat((C, more), dim=1)
+        el.C = E.Wavefunction(basis, coeff=C.contiguous()).orthonormalize()
+        return el
 
     @property
     def band_apps(self) -> int:

@@ -85,6 +85,21 @@ class Davidson:
         norm[i_k, i_b] = 1.0
 
     def __call__(self, n_iterations: Optional[int] = None) -> DavidsonStats:
+        """Run to convergence with direct H.psi calls."""
+        el = self.electrons
+        gen = self.steps(n_iterations)
+        block = next(gen)
+        while True:
+            try:
+                block = gen.send(el.hamiltonian(block))
+            except StopIteration as stop:
+                return stop.value
+
+    def steps(self, n_iterations: Optional[int] = None):
+        """The Davidson iteration as a generator: it yields every block of
+        vectors it needs H applied to and expects the H.psi result sent back;
+        its return value is the DavidsonStats.  A driver can therefore batch the
+        H.psi of many concurrent eigensolves (the serving loop does)."""
         el = self.electrons
         n_bands = el.n_bands
         n_bands_max = n_bands + el.n_bands_extra
@@ -93,8 +108,8 @@ class Davidson:
             raise ValueError(
                 f"n_bands + n_bands_extra = {n_bands_max} exceeds min(n_basis)/2 = {el.basis.n_min // 2} in Davidson"
             )
-        hpsi0 = el.hpsi_band_count
-        HC = el.hamiltonian(el.C)
+        hpsi_bands = el.C.n_bands() * el.basis.nk
+        HC = yield el.C
         el.eig, V = torch.linalg.eigh((el.C ^ HC).wait())  # _davidson.py:164-168
         el.deig_max = np.inf
         el.C = el.C @ V
@@ -120,7 +135,8 @@ class Davidson:
             Cnew = el.C.cat(Cexp)
             C_OC = torch.eye(n_bands_cur, device=V.device, dtype=torch.complex128)[None]
             C_OC_new = _tile_expansion(C_OC, (Cnew ^ Cexp).wait())
-            HCexp = el.hamiltonian(Cexp)
+            HCexp = yield Cexp
+            hpsi_bands += n_bands_exp * el.basis.nk
             C_HC = torch.diag_embed(el.eig).to(torch.complex128)
             C_HC_new = _tile_expansion(C_HC, (Cnew ^ HCexp).wait())
             eig_new, V_new = eighg(C_HC_new, C_OC_new)
@@ -141,7 +157,8 @@ class Davidson:
             if converged and self.residual_threshold is not None:
                 # HC is carried by rotations and drifts from H C over many
                 # iterations; test residuals against a fresh H C.
-                HC = el.hamiltonian(el.C)
+                HC = yield el.C
+                hpsi_bands += el.C.n_bands() * el.basis.nk
                 res = (HC - el.C * el.eig[..., None].to(el.C.coeff.real.dtype)).band_norm()
                 res_max = float(res[:, :n_bands].max())
                 if res_max >= self.residual_threshold:
@@ -150,7 +167,7 @@ class Davidson:
             if converged:
                 break
         self._HC = HC
-        return DavidsonStats(self._i_iter, converged, el.deig_max, res_max, el.hpsi_band_count - hpsi0)
+        return DavidsonStats(self._i_iter, converged, el.deig_max, res_max, hpsi_bands)
 
 
 def refine_fp64(el_mixed: Electrons, el_fp64: Electrons, C: Optional[Wavefunction] = None,

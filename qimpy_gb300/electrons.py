@@ -43,7 +43,7 @@ class Basis:
     """Plane-wave basis of one cell at all its k-points, resident on one GPU."""
 
     def __init__(self, Rbasis, k, wk, ke_cutoff: float, grid_shape, device="cuda",
-                 dtype: torch.dtype = torch.complex128, fft_factors=None):
+                 dtype: torch.dtype = torch.complex128, fft_factors=None, layout=None):
         Rbasis = np.asarray(Rbasis, dtype=np.float64)
         self.Rbasis = Rbasis
         self.Gbasis = 2.0 * np.pi * np.linalg.inv(Rbasis.T)
@@ -54,7 +54,7 @@ class Basis:
         self.grid_shape = tuple(int(x) for x in grid_shape)
         self.device = torch.device(device)
         self.dtype = dtype
-        self.layout = wl.make_basis(self.Gbasis, self.k, self.ke_cutoff, self.grid_shape)
+        self.layout = layout or wl.make_basis(self.Gbasis, self.k, self.ke_cutoff, self.grid_shape)
         self.n = self.layout.n
         self.n_tot = self.layout.n_tot
         self.n_min = int(self.n.min())

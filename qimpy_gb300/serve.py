@@ -1,0 +1,312 @@
+"""Continuous-batching eigensolve server on one GPU.
+
+Requests (a cell spec and a band count) arrive over time.  The server admits a
+queued request as soon as a slot and its HBM budget are free, keeps the
+request's wavefunctions, potential and projectors resident until it is done,
+and runs every active request's Davidson (the reference's algorithm,
+qimpy/dft/electrons/_davidson.py:141-235, stepped as a generator) in lock
+step: each server tick gathers the block every active request needs H applied
+to and runs them all as one batched H.psi (local potential in three launches
+per grid shape, nonlocal per request), then advances each request.  Requests
+that arrive while others are on the GPU join at the next tick, so their work
+overlaps on the device.  A mixed-precision request finishes with FP64
+refinement sweeps.  A request that fails (bad size, non-finite result,
+iteration limit) is reported with its error and leaves the others untouched.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib, ops
+from .batch import Instance, InstanceSpec
+from .davidson import Davidson, refine_fp64
+from .electrons import Wavefunction
+
+
+@dataclass
+class EigenRequest:
+    """One eigensolve: lowest `n_bands` eigenpairs of the cell in `spec`."""
+
+    rid: int
+    spec: InstanceSpec
+    n_bands: int
+    arrival: float = 0.0  #: seconds after the stream starts
+    status: str = "queued"  #: queued, active, done, failed, rejected
+    eig: Optional[np.ndarray] = None  #: (nk, n_bands) FP64
+    error: str = ""
+    t_admit: float = math.nan
+    t_done: float = math.nan
+    iterations: int = 0
+    hpsi_bands: int = 0
+    converged: bool = False
+    residual: float = math.nan
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+
+@dataclass
+class _Active:
+    req: EigenRequest
+    inst: Instance
+    el: object
+    gen: object
+    block: Wavefunction
+    planes: torch.Tensor
+    nbytes: int
+    sphere_dev: torch.Tensor
+
+
+class EigenServer:
+    """Continuous batching of Davidson eigensolves (see the module docstring)."""
+
+    def __init__(self, device="cuda", precision: str = "mixed", hbm_budget_bytes: int = 160 << 30,
+                 max_active: int = 64, eig_threshold: float = 1e-6, residual_threshold: Optional[float] = 1e-6,
+                 max_iterations: int = 200, refine: bool = True):
+        if precision not in ("mixed", "fp64"):
+            raise ValueError("precision must be 'mixed' or 'fp64'")
+        self.device = torch.device(device)
+        self.precision = precision
+        self.dtype = torch.complex64 if precision == "mixed" else torch.complex128
+        self.qdtype = _lib.QGB_F32 if precision == "mixed" else _lib.QGB_F64
+        self.budget = int(hbm_budget_bytes)
+        self.max_active = int(max_active)
+        self.eig_threshold = eig_threshold
+        self.residual_threshold = residual_threshold
+        self.max_iterations = max_iterations
+        self.refine = refine and precision == "mixed"
+        self.queue: list = []
+        self.active: list = []
+        self.finished: list = []
+        self.in_use = 0
+        self.ticks = 0
+        self.tick_band_apps: list = []
+
+    # ------------------------------------------------------------------ admission
+    def estimate_bytes(self, spec: InstanceSpec, n_bands: int) -> int:
+        """HBM held by an active request: wavefunction-sized Davidson arrays, the
+        slab planes of one block, projectors (and their bf16 operands), V, tables."""
+        from .batch import reference_grid  # noqa: F401  (grid already in spec)
+
+        N = spec.grid
+        nk = len(spec.k)
+        n_est = (2.0 * spec.ke_cutoff) ** 1.5 * spec.side ** 3 / (6 * math.pi ** 2) * 1.1
+        nbt = n_bands + max(1, math.ceil(0.1 * n_bands))
+        elem = 8 if self.dtype == torch.complex64 else 16
+        wf = 12 * nk * nbt * n_est * elem
+        planes = nk * nbt * (N // 2 + 2) * N * N * elem
+        P = 4 * spec.n_atoms
+        proj = nk * P * n_est * (elem + (8 if self.dtype == torch.complex64 else 0))
+        return int(wf + planes + proj + 4 * N ** 3 * 8)
+
+    def submit(self, req: EigenRequest) -> None:
+        self.queue.append(req)
+        self.queue.sort(key=lambda r: r.arrival)
+
+    def _admit(self, horizon: float, now: float) -> None:
+        """Admit queued requests that arrived by `horizon` while slots and memory allow."""
+        while self.queue and self.queue[0].arrival <= horizon and len(self.active) < self.max_active:
+            req = self.queue[0]
+            need = self.estimate_bytes(req.spec, req.n_bands)
+            if need > self.budget:
+                self.queue.pop(0)
+                self._reject(req, f"needs {need / 2**30:.1f} GiB > budget {self.budget / 2**30:.1f} GiB", now)
+                continue
+            if self.in_use + need > self.budget and self.active:
+                return  # wait for memory to free up
+            self.queue.pop(0)
+            try:
+                inst = Instance(req.spec, self.device, dtype=self.dtype)
+                nbt = req.n_bands + max(1, math.ceil(0.1 * req.n_bands))
+                n_min = int(inst.layout.n.min())
+                if req.n_bands < 1 or 2 * nbt >= n_min:  # Davidson's own limit (_davidson.py:159-163)
+                    raise ValueError(f"n_bands + n_bands_extra = {nbt} exceeds min(n_basis)/2 = {n_min // 2}")
+                el = inst.electrons(req.n_bands)
+                dav = Davidson(el, n_iterations=self.max_iterations, eig_threshold=self.eig_threshold,
+                               residual_threshold=None if self.refine else self.residual_threshold)
+                gen = dav.steps()
+                block = next(gen)
+            except (ValueError, RuntimeError) as e:
+                self._reject(req, str(e), now)
+                continue
+            planes = torch.empty(inst.sphere.workspace_bytes(el.C.n_bands(), budget=1 << 62), dtype=torch.uint8,
+                                 device=self.device)
+            sd = torch.frombuffer(bytearray(bytes(inst.sphere.struct)), dtype=torch.uint8).to(self.device)
+            req.status, req.t_admit = "active", now
+            self.active.append(_Active(req, inst, el, gen, block, planes, need, sd))
+            self.in_use += need
+
+    def _reject(self, req: EigenRequest, why: str, now: float) -> None:
+        req.status, req.error, req.t_done = "rejected", why, now
+        self.finished.append(req)
+
+    # ------------------------------------------------------------------ batched H.psi
+    def _batched_hamiltonian(self, acts: list) -> list:
+        """H applied to every active request's pending block: the local potential
+        of all requests sharing a grid shape in three batched launches, then each
+        request's nonlocal term."""
+        lib = _lib.lib()
+        outs = [torch.empty_like(a.block.coeff) for a in acts]
+        groups: dict = {}
+        for i, a in enumerate(acts):
+            groups.setdefault(a.inst.tables.shape, []).append(i)
+        st = torch.cuda.current_stream().cuda_stream
+        for idx in groups.values():
+            items = (_lib.QgbBatchItem * len(idx))()
+            slab_units, row_units, smem = [0], [0], 0
+            for j, i in enumerate(idx):
+                a = acts[i]
+                t = a.inst.tables
+                nb = a.block.n_bands()
+                items[j].sphere = a.sphere_dev.data_ptr()
+                items[j].C = a.block.coeff.data_ptr()
+                items[j].out = outs[i].data_ptr()
+                items[j].planes = a.planes.data_ptr()
+                items[j].nb = nb
+                items[j].flags = _lib.QGB_ADD_KE
+                slab_units.append(slab_units[-1] + t.nk * nb * t.max_slabs)
+                row_units.append(row_units[-1] + t.nk * nb * t.shape[1])
+                smem = max(smem, int(lib.qgb_sphere_smem_bytes(ct.byref(a.inst.sphere.struct), self.qdtype)))
+            ids = np.arange(len(idx), dtype=np.int32)
+            dev_items = torch.frombuffer(bytearray(bytes(items)), dtype=torch.uint8).to(self.device)
+            starts_s = torch.tensor(slab_units, dtype=torch.int64, device=self.device)
+            starts_r = torch.tensor(row_units, dtype=torch.int64, device=self.device)
+            item_s = torch.from_numpy(np.repeat(ids, np.diff(slab_units))).to(self.device)
+            item_r = torch.from_numpy(np.repeat(ids, np.diff(row_units))).to(self.device)
+            _lib.check(lib.qgb_apply_potential_batched(dev_items.data_ptr(), len(idx), item_s.data_ptr(),
+                                                       starts_s.data_ptr(), item_r.data_ptr(), starts_r.data_ptr(),
+                                                       slab_units[-1], row_units[-1], self.qdtype, smem, st),
+                       "apply_potential_batched")
+            for i in idx:
+                a, C = acts[i], acts[i].block.coeff
+                ions = a.el.ions
+                if self.dtype == torch.complex64:
+                    ops.apply_nonlocal_tc(ions.beta_split, ions.D, C, outs[i])
+                else:
+                    projT = ops.project(ions.beta, C)
+                    ops.apply_nonlocal(ions.beta, ions.D, projT, outs[i])
+        return [Wavefunction(a.el.basis, coeff=o) for a, o in zip(acts, outs)]
+
+    # ------------------------------------------------------------------ main loop
+    def tick(self, now_fn) -> None:
+        if not self.active:
+            return
+        acts = list(self.active)
+        results = self._batched_hamiltonian(acts)
+        self.ticks += 1
+        self.tick_band_apps.append(sum(a.block.n_bands() * a.inst.nk for a in acts))
+        for a, HC in zip(acts, results):
+            try:
+                a.block = a.gen.send(HC)
+            except StopIteration as stop:
+                self._finish(a, stop.value, now_fn)
+            except (ValueError, RuntimeError) as e:  # e.g. a non positive-definite overlap
+                self._fail(a, str(e), now_fn())
+
+    def _finish(self, a: _Active, stats, now_fn) -> None:
+        req, el = a.req, a.el
+        try:
+            eig = el.eig
+            if self.refine:
+                inst64 = Instance(req.spec, self.device, dtype=torch.complex128)
+                el64 = inst64.electrons(req.n_bands)
+                eig, _ = refine_fp64(el, el64, eig_threshold=min(1e-8, self.eig_threshold))
+                rs = el64.last_refine
+                req.hpsi_bands += rs.hpsi_bands
+                if self.residual_threshold is not None:
+                    HC = el64.hamiltonian(el64.C)
+                    res = (HC - el64.C * el64.eig[..., None]).band_norm()
+                    req.residual = float(res[:, : req.n_bands].max())
+                del inst64, el64
+            eig = eig[:, : req.n_bands].detach().cpu().numpy()
+            if not np.all(np.isfinite(eig)):
+                raise RuntimeError("non-finite eigenvalues")
+            req.eig, req.iterations, req.converged = eig, stats.iterations, bool(stats.converged)
+            req.hpsi_bands += stats.hpsi_bands
+            req.status = "done" if stats.converged else "failed"
+            if not stats.converged:
+                req.error = f"not converged in {stats.iterations} iterations (deig_max {stats.deig_max:.2e})"
+        except (ValueError, RuntimeError) as e:
+            req.status, req.error = "failed", str(e)
+        req.t_done = now_fn()
+        self._release(a)
+
+    def _fail(self, a: _Active, why: str, now: float) -> None:
+        a.req.status, a.req.error, a.req.t_done = "failed", why, now
+        self._release(a)
+
+    def _release(self, a: _Active) -> None:
+        self.active.remove(a)
+        self.in_use -= a.nbytes
+        self.finished.append(a.req)
+
+    def run(self, requests: list, realtime: bool = True, max_wall_s: float = 3600.0) -> dict:
+        """Serve `requests` (arrival times in seconds from now) to completion.
+
+        realtime=True follows the wall clock (a request is admitted only once its
+        arrival time has passed); realtime=False admits requests in arrival order
+        as soon as slots and memory allow."""
+        for r in requests:
+            self.submit(r)
+        t0 = time.perf_counter()
+
+        def now() -> float:
+            return time.perf_counter() - t0
+
+        while self.queue or self.active:
+            t = now()
+            self._admit(t if realtime else math.inf, t)
+            if not self.active:
+                if not self.queue:
+                    break
+                wait = self.queue[0].arrival - now()
+                if wait > 0:
+                    time.sleep(min(wait, 0.01))
+                continue
+            self.tick(now)
+            torch.cuda.synchronize()
+            if now() > max_wall_s:
+                for a in list(self.active):
+                    self._fail(a, "server time limit", now())
+                for r in self.queue:
+                    self._reject(r, "server time limit", now())
+                self.queue.clear()
+        return self.report(now())
+
+    def report(self, wall: float) -> dict:
+        done = [r for r in self.finished if r.status == "done"]
+        lat = np.array([r.latency for r in done]) if done else np.array([math.nan])
+        first = min((r.arrival for r in self.finished), default=0.0)
+        last = max((r.t_done for r in done), default=first)
+        return dict(requests=len(self.finished), done=len(done),
+                    failed=sum(r.status == "failed" for r in self.finished),
+                    rejected=sum(r.status == "rejected" for r in self.finished),
+                    eigensolves_per_s=len(done) / max(last - first, 1e-9), wall_s=wall,
+                    p50_latency_s=float(np.percentile(lat, 50)), p99_latency_s=float(np.percentile(lat, 99)),
+                    ticks=self.ticks, mean_band_apps_per_tick=float(np.mean(self.tick_band_apps)) if self.ticks else 0.0,
+                    hpsi_band_apps=int(sum(r.hpsi_bands for r in done)))
+
+
+def poisson_stream(specs: list, rate_hz: float, seed: int, bands_choices=(8, 16, 32, 64, 96, 128, 160)) -> list:
+    """Requests with exponential inter-arrival times (mean 1/rate) over `specs`;
+    each asks for a band count drawn from bands_choices (capped so that
+    2 (n_bands + extra) stays below the basis size)."""
+    from .workloads import splitmix_uniform
+
+    u = splitmix_uniform(seed, 77, 2 * len(specs))
+    t, reqs = 0.0, []
+    for i, spec in enumerate(specs):
+        t += -math.log(u[2 * i]) / rate_hz
+        nb = bands_choices[int(u[2 * i + 1] * len(bands_choices)) % len(bands_choices)]
+        n_est = (2.0 * spec.ke_cutoff) ** 1.5 * spec.side ** 3 / (6 * math.pi ** 2)
+        nb = int(min(nb, max(4, 0.3 * n_est)))
+        reqs.append(EigenRequest(i, spec, nb, arrival=t))
+    return reqs
