@@ -195,7 +195,7 @@ class Instance:
                                              device=self.sphere.device),
                                  torch.randn((self.nk, n_bands + extra - C.shape[1], self.n_tot), generator=g,
                                              device=self.sphere.device)).to(self.dtype)
-            more = more / (1 + basis.ke[:, None, :]) * basis.mask[:, None, :]
+            more = (more / (1 + basis.ke[:, None, :]) * basis.mask[:, None, :]).to(self.dtype)
             C = torch.cat((C, more), dim=1)
         el.C = E.Wavefunction(basis, coeff=C.contiguous()).orthonormalize()
         return el
@@ -212,6 +212,10 @@ class _Group:
     def __init__(self, instances: list, inputs: list, outputs: list, device):
         lib = _lib.lib()
         self.instances, self.inputs, self.outputs = instances, inputs, outputs
+        for inst, c, o in zip(instances, inputs, outputs):
+            if c.dtype != torch.complex64 or o.dtype != torch.complex64 or c.shape != (inst.nk, inst.nb, inst.n_tot) \
+                    or o.shape != c.shape or not (c.is_contiguous() and o.is_contiguous()):
+                raise TypeError("batched instances need contiguous complex64 (nk, nb, n_tot) inputs and outputs")
         n = len(instances)
         ssz = ct.sizeof(_lib.QgbSphere)
         host = bytearray(ssz * n)

@@ -154,6 +154,12 @@ class EigenServer:
         of all requests sharing a grid shape in three batched launches, then each
         request's nonlocal term."""
         lib = _lib.lib()
+        for a in acts:  # the kernels read every block with the server's element type
+            c = a.block.coeff
+            if c.dtype != self.dtype or not c.is_contiguous() or c.shape[0] != a.inst.nk or c.shape[2] != a.inst.n_tot:
+                raise TypeError(f"request {a.req.rid}: block {tuple(c.shape)} {c.dtype} does not match its sphere")
+            if c.shape[1] * a.inst.sphere.workspace_bytes(1, budget=1 << 62) > a.planes.numel():
+                raise ValueError(f"request {a.req.rid}: block of {c.shape[1]} bands exceeds its plane workspace")
         outs = [torch.empty_like(a.block.coeff) for a in acts]
         groups: dict = {}
         for i, a in enumerate(acts):
