@@ -442,7 +442,8 @@ def run_batch(args, local):
 
 def run_serving(args, local):
     """Continuous-batching eigensolve server: a Poisson stream (mean 200 req/s)
-    of requests for the lowest N_bands in {8..160} eigenpairs (residual 1e-6),
+    of requests for the lowest N_bands in {8..160} eigenpairs (eigenvalue change
+    below 1e-6 Ha; mixed requests then refined in FP64 to 1e-8 Ha),
     cells drawn from the batched-instance distribution plus 5% 64-atom Si-like
     cells (side 20.52 bohr, 96^3, Ecut 20 Ha).  Mixed precision (FP32 H.psi,
     tensor-core nonlocal, FP64 subspace and refinement) and plain FP64; a
@@ -462,9 +463,10 @@ def run_serving(args, local):
                 pos = wl.supercell_positions(wl._DIAMOND_BASIS, 2)
                 specs[i] = bt.InstanceSpec(i, 20.52, pos, 20.0, 160, np.zeros((1, 3)), 41 * 100003 + i, grid=96)
         reqs = sv.poisson_stream(specs, rate_hz=200.0, seed=41)
-        srv = sv.EigenServer(dev, precision=precision, eig_threshold=1e-6, residual_threshold=1e-6)
+        srv = sv.EigenServer(dev, precision=precision, eig_threshold=1e-6)
         rep = srv.run(reqs, realtime=True, max_wall_s=args.serve_wall)
-        rep["residual_max"] = float(np.nanmax([r.residual for r in reqs])) if precision == "mixed" else None
+        res = [r.residual for r in reqs if r.status == "done"]
+        rep["residual_max"] = float(np.max(res)) if res else None
         rep["sample"] = f"{count} requests of the 200 req/s stream ({sum(u < 0.05)} Si64-like)"
         out[precision] = rep
     out["mixed_over_fp64_eigensolves"] = out["mixed"]["eigensolves_per_s"] / max(out["fp64"]["eigensolves_per_s"], 1e-12)

@@ -40,7 +40,8 @@ enum qgb_status {
   QGB_ERR_WORKSPACE = 2,   /* workspace smaller than qgb_*_workspace_bytes() */
   QGB_ERR_CUDA = 3,        /* CUDA runtime or launch error */
   QGB_ERR_CUBLAS = 4,      /* cuBLAS error */
-  QGB_ERR_UNSUPPORTED = 5  /* valid request this build does not implement */
+  QGB_ERR_UNSUPPORTED = 5, /* valid request this build does not implement */
+  QGB_ERR_CUSOLVER = 6     /* cuSOLVER error */
 };
 
 /* Flags of qgb_apply_potential. */
@@ -255,6 +256,19 @@ int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, 
 int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N,
                        int K, int lda, int ldb, float* D, int* dev_error, void* workspace,
                        size_t workspace_bytes, void* stream);
+
+/*
+ * FP64 eigenpairs of nk Hermitian n x n matrices A ([nk][n][n] complex128,
+ * row-major) in one batched cuSOLVER call on `stream`: W [nk][n] ascending
+ * eigenvalues; A is overwritten with V^H (row j = conj of eigenvector j);
+ * info [nk] device ints, nonzero where a matrix failed to converge.
+ * Workspace of qgb_subspace_eigh_workspace_bytes(nk, n) (0 = query failed).
+ * Replaces the torch.linalg.eigh of the Davidson subspace problems
+ * (qimpy/dft/electrons/_davidson.py:164-168; qimpy/math/_linalg.py:143-183).
+ */
+size_t qgb_subspace_eigh_workspace_bytes(int64_t nk, int64_t n);
+int qgb_subspace_eigh(void* A, double* W, int* info, int64_t nk, int64_t n, void* workspace,
+                      size_t workspace_bytes, void* stream);
 
 /*
  * Diagnostic: `blocks` x `threads` threads each run 8 independent FMA chains

@@ -18,7 +18,7 @@ QGB_ADD_KE, QGB_ACCUMULATE = 1, 2
 ABI_VERSION = 1
 
 _ERRORS = {1: "invalid argument", 2: "workspace too small", 3: "CUDA error", 4: "cuBLAS error",
-           5: "unsupported"}
+           5: "unsupported", 6: "cuSOLVER error"}
 
 
 class QgbSphere(ct.Structure):
@@ -82,6 +82,9 @@ _SIGS = {
     "qgb_hamiltonian_mixed": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p,
                                          ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_size_t,
                                          ct.c_void_p, ct.c_void_p]),
+    "qgb_subspace_eigh_workspace_bytes": (ct.c_size_t, [ct.c_int64, ct.c_int64]),
+    "qgb_subspace_eigh": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64, ct.c_void_p,
+                                     ct.c_size_t, ct.c_void_p]),
     "qgb_tc_gemm_bf16x3": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
                                       ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                       ct.c_size_t, ct.c_void_p]),

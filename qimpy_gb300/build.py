@@ -1,7 +1,7 @@
 """Build ``libqimpy_gb300.so`` in-tree for sm_103a (GB300).
 
 Each ``csrc/*.cu`` is compiled by nvcc in parallel into ``_build/``, then
-linked with cuBLAS into ``qimpy_gb300/libqimpy_gb300.so``.  The DFT codelet
+linked with cuBLAS and cuSOLVER into ``qimpy_gb300/libqimpy_gb300.so``.  The DFT codelet
 header is regenerated when its generator is newer.  Rebuilds only what changed.
 """
 from __future__ import annotations
@@ -80,7 +80,7 @@ def build(force: bool = False, verbose: bool = False, debug: bool = False) -> st
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra, build_dir), srcs))
     if force or _mtime(lib) < max(_mtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs + ["-lcublas"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs + ["-lcublas", "-lcusolver"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -7,6 +7,11 @@ eigenvalue change).  Additions:
 
 * an optional residual-norm stop (max_b ||H psi_b - eps_b psi_b|| over the
   first n_bands, in FP64) beside the reference's eigenvalue-change stop;
+* for FP32 (mixed-precision) vectors: span(C) projected out of the
+  expansion vectors (same subspace, better conditioned), canonical
+  orthogonalisation of the expanded basis where its overlap is still too
+  ill-conditioned for FP32 (directions below 1e-4 of the overlap dropped), and
+  a stop at FP32's floor that leaves the rest to the FP64 refinement;
 * ``refine_fp64``: FP64 refinement of a mixed-precision solve (Cholesky
   orthonormalisation, then FP64 Davidson sweeps: FP64 H.psi, Rayleigh-Ritz,
   residual expansion, expanded Rayleigh-Ritz).
@@ -20,7 +25,7 @@ import numpy as np
 import torch
 
 from .electrons import Electrons, Wavefunction
-from .linalg import eighg
+from .linalg import eigh, eighg
 
 
 @dataclass
@@ -30,6 +35,9 @@ class DavidsonStats:
     deig_max: float
     residual_max: float
     hpsi_bands: int
+    #: FP32 only: stopped at the precision floor (basis too ill-conditioned for
+    #: FP32, or eigenvalue changes growing again); el holds the last good state.
+    stalled: bool = False
 
 
 def _tile_expansion(C_XC: torch.Tensor, Cnew_XCexp: torch.Tensor) -> torch.Tensor:
@@ -110,7 +118,7 @@ class Davidson:
             )
         hpsi_bands = el.C.n_bands() * el.basis.nk
         HC = yield el.C
-        el.eig, V = torch.linalg.eigh((el.C ^ HC).wait())  # _davidson.py:164-168
+        el.eig, V = eigh((el.C ^ HC).wait())  # _davidson.py:164-168
         el.deig_max = np.inf
         el.C = el.C @ V
         HC = HC @ V
@@ -118,6 +126,9 @@ class Davidson:
         converged = False
         res_max = np.inf
         self._i_iter = 0
+        fp32 = el.C.coeff.dtype == torch.complex64
+        stalled = False
+        min_deig, i_best = np.inf, 0
         for self._i_iter in range(1, n_iterations + 1):
             n_bands_cur = el.C.n_bands()
             eig_sel = el.eig[:, n_eigs_done:, None]
@@ -126,6 +137,14 @@ class Davidson:
             KEref = C_sel.band_ke()
             R = HC_sel - C_sel * eig_sel.to(C_sel.coeff.real.dtype)
             Cexp = self.precondition(R, KEref)
+            if fp32:
+                # Project span(C) out of the expansion (twice: classical
+                # Gram-Schmidt with re-orthogonalisation).  span(C, Cexp) and
+                # hence the Ritz pairs are unchanged, but near convergence the
+                # new directions are a small part of Cexp, and keeping the rest
+                # would leave the overlap too ill-conditioned for FP32.
+                for _ in range(2):
+                    Cexp = Cexp - el.C @ (el.C ^ Cexp).wait()
             norm_exp = Cexp.band_norm()
             self._regularize(Cexp, norm_exp, self._i_iter)
             Cexp *= (1.0 / norm_exp)
@@ -139,8 +158,16 @@ class Davidson:
             hpsi_bands += n_bands_exp * el.basis.nk
             C_HC = torch.diag_embed(el.eig).to(torch.complex128)
             C_HC_new = _tile_expansion(C_HC, (Cnew ^ HCexp).wait())
-            eig_new, V_new = eighg(C_HC_new, C_OC_new)
+            # FP32 vectors: directions the expanded basis barely spans are below
+            # its rounding and are dropped (canonical orthogonalisation).
+            eig_new, V_new = eighg(C_HC_new, C_OC_new, drop_below=1e-4 if fp32 else 0.0)
             n_bands_next = min(n_bands_new, n_bands_max)
+            if fp32 and bool(torch.isinf(eig_new[:, n_bands_next - 1]).any()):
+                # Fewer usable directions than retained bands: no usable update
+                # at FP32 precision.  Keep the current state.
+                stalled = True
+                break
+            prev = (el.C, el.eig, HC, el.deig_max)
             V_new = V_new[..., :n_bands_next]
             Vcur, Vexp = V_new[:, :n_bands_cur], V_new[:, n_bands_cur:]
             el.C = Cnew @ V_new
@@ -151,6 +178,13 @@ class Davidson:
             # _check_deig (_davidson.py:126-139), one host sync per iteration:
             d = deig[:, :n_bands]
             el.deig_max = float(d.max())
+            if fp32 and min_deig < 1e-3 and el.deig_max > 100.0 * min_deig:
+                # FP32 rounding has started to feed back: revert and stop.
+                el.C, el.eig, HC, el.deig_max = prev
+                stalled = True
+                break
+            if el.deig_max < min_deig:
+                min_deig, i_best = el.deig_max, self._i_iter
             pending = torch.where((d > self.eig_threshold).any(dim=0))[0]
             n_eigs_done = int(pending[0]) if len(pending) else n_bands
             converged = n_eigs_done >= n_bands
@@ -166,12 +200,15 @@ class Davidson:
                     n_eigs_done = 0  # eigenvalues settled, residuals not yet: keep all bands active
             if converged:
                 break
+            if fp32 and self._i_iter - i_best >= 10:
+                stalled = True  # no progress for 10 iterations: FP32's floor
+                break
         self._HC = HC
-        return DavidsonStats(self._i_iter, converged, el.deig_max, res_max, hpsi_bands)
+        return DavidsonStats(self._i_iter, converged, el.deig_max, res_max, hpsi_bands, stalled)
 
 
 def refine_fp64(el_mixed: Electrons, el_fp64: Electrons, C: Optional[Wavefunction] = None,
-                eig_threshold: float = 1e-8, max_sweeps: int = 8):
+                eig_threshold: float = 1e-8, max_sweeps: int = 40, residual_threshold: Optional[float] = None):
     """FP64 refinement of mixed-precision eigenvectors.
 
     Upcasts the vectors to complex128, orthonormalises them (Cholesky, FP64),
@@ -181,10 +218,12 @@ def refine_fp64(el_mixed: Electrons, el_fp64: Electrons, C: Optional[Wavefunctio
     FP32 H.psi leaves eigenvalues with noise near eps_f32 * Ecut (~1e-6 Ha);
     the FP64 sweeps remove it.  Returns (eigenvalues (nk, nb) FP64, refined FP64
     Wavefunction); el_fp64 holds the refined state and `el_fp64.last_refine`
-    the sweep statistics."""
+    the sweep statistics.  With `residual_threshold` the sweeps also continue
+    until every band's FP64 residual norm is below it (at most `max_sweeps`)."""
     C = C or el_mixed.C
     C64 = Wavefunction(el_fp64.basis, coeff=C.coeff.to(torch.complex128))
     C64.constrain()
     el_fp64.C = C64.orthonormalize()
-    el_fp64.last_refine = Davidson(el_fp64, n_iterations=max_sweeps, eig_threshold=eig_threshold)()
+    el_fp64.last_refine = Davidson(el_fp64, n_iterations=max_sweeps, eig_threshold=eig_threshold,
+                                   residual_threshold=residual_threshold)()
     return el_fp64.eig, el_fp64.C

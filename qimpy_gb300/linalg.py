@@ -1,12 +1,49 @@
-"""Subspace linear algebra in FP64 on the GPU (cuSOLVER through torch.linalg).
+"""Subspace linear algebra in FP64 on the GPU.
 
 Restates qimpy/math/_linalg.py:110-183 (``ortho_matrix``, ``eighg``): the
-Cholesky orthonormaliser U = (L^-1)^H of the overlap O, then eigh of U^H H U.
-Both precision forms keep these steps in FP64.
+Cholesky orthonormaliser U = (L^-1)^H of the overlap O (cuSOLVER through
+torch.linalg), then eigh of U^H H U through the library's batched cuSOLVER
+entry point (qgb_subspace_eigh: all k-points in one call).  Both precision
+forms keep these steps in FP64.
 """
 from __future__ import annotations
 
+import ctypes as ct
+import math
+
 import torch
+
+from . import _lib
+
+
+def eigh(A: torch.Tensor):
+    """Eigenvalues (ascending) and eigenvectors of Hermitian FP64 matrices
+    A [..., n, n] on a CUDA device, one batched cuSOLVER call
+    (qgb_subspace_eigh) for all leading indices.  Raises if any fails to
+    converge (as torch.linalg.eigh does)."""
+    if A.device.type != "cuda" or A.dtype != torch.complex128:
+        raise TypeError(f"eigh needs complex128 CUDA matrices, got {A.dtype} on {A.device}")
+    n = A.shape[-1]
+    lead = A.shape[:-2]
+    X = A.reshape(-1, n, n).clone(memory_format=torch.contiguous_format)
+    nk = X.shape[0]
+    W = torch.empty((nk, n), dtype=torch.float64, device=A.device)
+    if nk == 0 or n == 0:
+        return W.reshape(*lead, n), X.reshape(*lead, n, n)
+    info = torch.empty(nk, dtype=torch.int32, device=A.device)
+    lib = _lib.lib()
+    ws_bytes = int(lib.qgb_subspace_eigh_workspace_bytes(nk, n))
+    if ws_bytes == 0:
+        raise _lib.QgbError(f"subspace_eigh workspace query failed: {lib.qgb_last_error().decode()}")
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=A.device)
+    st = torch.cuda.current_stream(A.device).cuda_stream
+    _lib.check(lib.qgb_subspace_eigh(X.data_ptr(), W.data_ptr(), info.data_ptr(), nk, n, ws.data_ptr(),
+                                     ws_bytes, ct.c_void_p(st)), "subspace_eigh")
+    bad = torch.nonzero(info).flatten().tolist()
+    if bad:
+        raise RuntimeError(f"subspace eigh: (Batch element {bad[0]}) did not converge (info {int(info[bad[0]])})")
+    # X holds V^H row-major (the column-major solve saw conj(A)).
+    return W.reshape(*lead, n), X.conj().transpose(-2, -1).reshape(*lead, n, n)
 
 
 def dagger(x: torch.Tensor) -> torch.Tensor:
@@ -18,13 +55,56 @@ def ortho_matrix(O: torch.Tensor, use_cholesky: bool = True) -> torch.Tensor:
     if use_cholesky:
         eye = torch.eye(O.shape[-1], device=O.device, dtype=O.dtype).expand(O.shape)
         return dagger(torch.linalg.solve_triangular(torch.linalg.cholesky(O), eye, upper=False))
-    lbda, V = torch.linalg.eigh(O)
+    lbda, V = eigh(O)
     return V @ ((1.0 / torch.sqrt(lbda))[..., None] * dagger(V))
 
 
-def eighg(H, O: torch.Tensor, use_cholesky: bool = True):
-    """Solve H V = O V E (qimpy/math/_linalg.py:143-183); H may be a Waitable."""
-    U = ortho_matrix(O, use_cholesky)
+def _canonical_ortho(O: torch.Tensor, drop_below: float):
+    """Canonical orthogonalisation (Loewdin, Int. J. Quantum Chem. 4, 1970):
+    U = V_kept diag(lambda_kept^-1/2) from the eigenpairs of O, dropping the
+    directions with lambda < drop_below * max_i O_ii.  Dropped columns of U are
+    zero, so U keeps its square shape across the batch; `keep` marks the rest."""
+    lbda, V = eigh(O)
+    floor = drop_below * O.diagonal(dim1=-2, dim2=-1).real.amax(dim=-1, keepdim=True)
+    keep = lbda > floor
+    scale = torch.where(keep, 1.0 / torch.sqrt(torch.where(keep, lbda, torch.ones_like(lbda))),
+                        torch.zeros_like(lbda))
+    return V * scale[..., None, :].to(V.dtype), keep
+
+
+def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0):
+    """Solve H V = O V E (qimpy/math/_linalg.py:143-183); H may be a Waitable.
+
+    drop_below > 0 is for overlaps of FP32 vectors.  Their rounding (and the
+    drift of supposedly orthonormal vectors) is ~1e-5 of O, so directions the
+    subspace barely spans cannot be resolved: Cholesky fails on them, or
+    amplifies their noise by lambda^-1/2.  When the Cholesky pivots show such a
+    direction (min L_ii^2 < drop_below * max O_ii, or a failed factorisation),
+    the basis is orthonormalised canonically instead, dropping directions with
+    eigenvalue below that floor.  Dropped directions come last, with
+    eigenvalue +inf and eigenvector zero."""
     Hr = H.wait() if hasattr(H, "wait") else H
-    E, V = torch.linalg.eigh(dagger(U) @ (Hr @ U))
+    keep = None
+    if drop_below > 0.0 and use_cholesky:
+        eye = torch.eye(O.shape[-1], device=O.device, dtype=O.dtype).expand(O.shape)
+        L, info = torch.linalg.cholesky_ex(O)
+        pivot = L.diagonal(dim1=-2, dim2=-1).real.square().amin(dim=-1)
+        floor = drop_below * O.diagonal(dim1=-2, dim2=-1).real.amax(dim=-1)
+        if bool(((info != 0) | (pivot < floor)).any()):
+            U, keep = _canonical_ortho(O, drop_below)
+        else:
+            U = dagger(torch.linalg.solve_triangular(L, eye, upper=False))
+    else:
+        U = ortho_matrix(O, use_cholesky)
+    Hs = dagger(U) @ (Hr @ U)
+    if keep is None:
+        E, V = eigh(Hs)
+        return E, U @ V
+    # Dropped directions: zero rows/columns of Hs; give them a diagonal above the
+    # spectral norm of the rest so that they sort last, then mark them +inf.
+    big = 10.0 * (torch.linalg.matrix_norm(Hs).amax() + 1.0)
+    Hs = Hs + torch.diag_embed((~keep).to(torch.float64) * big).to(Hs.dtype)
+    E, V = eigh(Hs)
+    n_keep = keep.sum(dim=-1, keepdim=True)
+    E = torch.where(torch.arange(E.shape[-1], device=E.device) >= n_keep, torch.full_like(E, math.inf), E)
     return E, U @ V

@@ -18,6 +18,8 @@ from __future__ import annotations
 import ctypes as ct
 import math
 import time
+import traceback
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -63,14 +65,23 @@ class _Active:
     planes: torch.Tensor
     nbytes: int
     sphere_dev: torch.Tensor
+    stream: torch.cuda.Stream
+    ready: torch.cuda.Event  #: recorded on `stream` after the request's last step
+    stats: object = None  #: DavidsonStats once the mixed/FP64 solve has finished
 
 
 class EigenServer:
     """Continuous batching of Davidson eigensolves (see the module docstring)."""
 
     def __init__(self, device="cuda", precision: str = "mixed", hbm_budget_bytes: int = 160 << 30,
-                 max_active: int = 64, eig_threshold: float = 1e-6, residual_threshold: Optional[float] = 1e-6,
-                 max_iterations: int = 200, refine: bool = True):
+                 max_active: int = 64, eig_threshold: float = 1e-6, residual_threshold: Optional[float] = None,
+                 max_iterations: int = 200, refine: bool = True, refine_threshold: float = 1e-8,
+                 workers: int = 16):
+        """eig_threshold: Davidson's stop on the largest eigenvalue change (Ha);
+        refine_threshold: the same for the FP64 refinement of a mixed solve;
+        residual_threshold: optional extra stop on the FP64 residual norm
+        (FP64 solve, or the refinement).  Every finished request reports its
+        final residual."""
         if precision not in ("mixed", "fp64"):
             raise ValueError("precision must be 'mixed' or 'fp64'")
         self.device = torch.device(device)
@@ -83,12 +94,36 @@ class EigenServer:
         self.residual_threshold = residual_threshold
         self.max_iterations = max_iterations
         self.refine = refine and precision == "mixed"
+        self.refine_threshold = refine_threshold
         self.queue: list = []
         self.active: list = []
         self.finished: list = []
         self.in_use = 0
         self.ticks = 0
         self.tick_band_apps: list = []
+        # Request steps (Davidson host logic, cuSOLVER subspace algebra, FP64
+        # refinement) run concurrently in worker threads, each request on its own
+        # CUDA stream; the batched H.psi runs on the server's stream.
+        self.workers = workers
+        self._pool = ThreadPoolExecutor(max_workers=workers)
+        # Finished solves (FP64 refinement, final residual) complete beside the
+        # next ticks on a pool of their own.
+        self._finisher = ThreadPoolExecutor(max_workers=max(1, workers // 4))
+        self._completing: list = []
+        self._warm_up()
+        self.tick_wall: list = []  #: host seconds per tick
+        self._hpsi_events: list = []  #: (start, end) CUDA events around each batched H.psi
+
+    def _warm_up(self) -> None:
+        """Load the extension and torch's lazily loaded linear-algebra backends
+        once on this thread: their first use from several worker threads at
+        once races inside torch."""
+        _lib.lib()
+        x = torch.eye(2, dtype=torch.complex128, device=self.device)[None] * 2.0
+        L, _ = torch.linalg.cholesky_ex(x)
+        torch.linalg.solve_triangular(L, x, upper=False)
+        torch.linalg.cholesky(x)
+        torch.cuda.synchronize(self.device)
 
     # ------------------------------------------------------------------ admission
     def estimate_bytes(self, spec: InstanceSpec, n_bands: int) -> int:
@@ -112,37 +147,57 @@ class EigenServer:
         self.queue.sort(key=lambda r: r.arrival)
 
     def _admit(self, horizon: float, now: float) -> None:
-        """Admit queued requests that arrived by `horizon` while slots and memory allow."""
-        while self.queue and self.queue[0].arrival <= horizon and len(self.active) < self.max_active:
+        """Admit queued requests that arrived by `horizon` while slots and memory
+        allow; their set-up (cell data, start vectors, first Davidson step) runs
+        in the worker pool."""
+        admitted = []
+        while self.queue and self.queue[0].arrival <= horizon and len(self.active) + len(admitted) < self.max_active:
             req = self.queue[0]
             need = self.estimate_bytes(req.spec, req.n_bands)
             if need > self.budget:
                 self.queue.pop(0)
                 self._reject(req, f"needs {need / 2**30:.1f} GiB > budget {self.budget / 2**30:.1f} GiB", now)
                 continue
-            if self.in_use + need > self.budget and self.active:
-                return  # wait for memory to free up
+            if self.in_use + need > self.budget and (self.active or admitted or self._completing):
+                break  # wait for memory to free up
             self.queue.pop(0)
-            try:
+            self.in_use += need
+            admitted.append((req, need))
+        main = torch.cuda.current_stream()
+        for req, need, result in zip([a[0] for a in admitted], [a[1] for a in admitted],
+                                     self._pool.map(lambda rn: self._setup(rn[0], main), admitted)):
+            if isinstance(result, Exception):
+                self.in_use -= need
+                self._reject(req, str(result), now)
+                continue
+            inst, el, gen, block, planes, sd, stream, ready = result
+            req.status, req.t_admit = "active", now
+            self.active.append(_Active(req, inst, el, gen, block, planes, need, sd, stream, ready))
+
+    def _setup(self, req: EigenRequest, main: torch.cuda.Stream):
+        stream = torch.cuda.Stream(device=self.device)
+        stream.wait_stream(main)
+        try:
+            with torch.cuda.stream(stream):
                 inst = Instance(req.spec, self.device, dtype=self.dtype)
                 nbt = req.n_bands + max(1, math.ceil(0.1 * req.n_bands))
                 n_min = int(inst.layout.n.min())
                 if req.n_bands < 1 or 2 * nbt >= n_min:  # Davidson's own limit (_davidson.py:159-163)
                     raise ValueError(f"n_bands + n_bands_extra = {nbt} exceeds min(n_basis)/2 = {n_min // 2}")
                 el = inst.electrons(req.n_bands)
+                precision_is_mixed = self.dtype == torch.complex64
                 dav = Davidson(el, n_iterations=self.max_iterations, eig_threshold=self.eig_threshold,
-                               residual_threshold=None if self.refine else self.residual_threshold)
+                               residual_threshold=None if precision_is_mixed else self.residual_threshold)
                 gen = dav.steps()
                 block = next(gen)
-            except (ValueError, RuntimeError) as e:
-                self._reject(req, str(e), now)
-                continue
-            planes = torch.empty(inst.sphere.workspace_bytes(el.C.n_bands(), budget=1 << 62), dtype=torch.uint8,
-                                 device=self.device)
-            sd = torch.frombuffer(bytearray(bytes(inst.sphere.struct)), dtype=torch.uint8).to(self.device)
-            req.status, req.t_admit = "active", now
-            self.active.append(_Active(req, inst, el, gen, block, planes, need, sd))
-            self.in_use += need
+                planes = torch.empty(inst.sphere.workspace_bytes(el.C.n_bands(), budget=1 << 62), dtype=torch.uint8,
+                                     device=self.device)
+                sd = torch.frombuffer(bytearray(bytes(inst.sphere.struct)), dtype=torch.uint8).to(self.device)
+                ready = torch.cuda.Event()
+                ready.record(stream)
+            return inst, el, gen, block, planes, sd, stream, ready
+        except (ValueError, RuntimeError, torch.cuda.OutOfMemoryError) as e:
+            return e
 
     def _reject(self, req: EigenRequest, why: str, now: float) -> None:
         req.status, req.error, req.t_done = "rejected", why, now
@@ -205,51 +260,105 @@ class EigenServer:
     def tick(self, now_fn) -> None:
         if not self.active:
             return
+        t0 = time.perf_counter()
         acts = list(self.active)
+        main = torch.cuda.current_stream()
+        for a in acts:  # blocks were produced on the requests' streams
+            main.wait_event(a.ready)
+            a.block.coeff.record_stream(main)
+        start_hpsi = torch.cuda.Event(enable_timing=True)
+        start_hpsi.record(main)
         results = self._batched_hamiltonian(acts)
+        done_hpsi = torch.cuda.Event(enable_timing=True)
+        done_hpsi.record(main)
+        self._hpsi_events.append((start_hpsi, done_hpsi))
         self.ticks += 1
         self.tick_band_apps.append(sum(a.block.n_bands() * a.inst.nk for a in acts))
-        for a, HC in zip(acts, results):
-            try:
-                a.block = a.gen.send(HC)
-            except StopIteration as stop:
-                self._finish(a, stop.value, now_fn)
-            except (ValueError, RuntimeError) as e:  # e.g. a non positive-definite overlap
-                self._fail(a, str(e), now_fn())
+        outcome = list(self._pool.map(lambda ar: self._advance(ar[0], ar[1], done_hpsi, now_fn), zip(acts, results)))
+        for a, (kind, payload) in zip(acts, outcome):
+            if kind == "finished":  # refinement and checks run beside the next ticks
+                self.active.remove(a)
+                self._completing.append((a, self._finisher.submit(self._complete, a, payload, now_fn)))
+            elif kind == "failed":
+                self._fail(a, payload, now_fn())
+        self.tick_wall.append(time.perf_counter() - t0)
 
-    def _finish(self, a: _Active, stats, now_fn) -> None:
-        req, el = a.req, a.el
+    def _reap(self, wait: bool = False) -> None:
+        """Release the memory of requests whose completion has finished."""
+        keep = []
+        for a, fut in self._completing:
+            if wait or fut.done():
+                fut.result()
+                a.stream.synchronize()
+                self.in_use -= a.nbytes
+                self.finished.append(a.req)
+            else:
+                keep.append((a, fut))
+        self._completing = keep
+
+    def _advance(self, a: _Active, HC: Wavefunction, done_hpsi, now_fn):
+        """One step of a request on its own stream (worker thread)."""
         try:
-            eig = el.eig
-            if self.refine:
-                inst64 = Instance(req.spec, self.device, dtype=torch.complex128)
-                el64 = inst64.electrons(req.n_bands)
-                eig, _ = refine_fp64(el, el64, eig_threshold=min(1e-8, self.eig_threshold))
-                rs = el64.last_refine
-                req.hpsi_bands += rs.hpsi_bands
-                if self.residual_threshold is not None:
-                    HC = el64.hamiltonian(el64.C)
-                    res = (HC - el64.C * el64.eig[..., None]).band_norm()
-                    req.residual = float(res[:, : req.n_bands].max())
-                del inst64, el64
-            eig = eig[:, : req.n_bands].detach().cpu().numpy()
-            if not np.all(np.isfinite(eig)):
-                raise RuntimeError("non-finite eigenvalues")
-            req.eig, req.iterations, req.converged = eig, stats.iterations, bool(stats.converged)
-            req.hpsi_bands += stats.hpsi_bands
-            req.status = "done" if stats.converged else "failed"
-            if not stats.converged:
-                req.error = f"not converged in {stats.iterations} iterations (deig_max {stats.deig_max:.2e})"
+            with torch.cuda.stream(a.stream):
+                a.stream.wait_event(done_hpsi)
+                HC.coeff.record_stream(a.stream)
+                try:
+                    a.block = a.gen.send(HC)
+                except StopIteration as stop:
+                    return ("finished", stop.value)
+                a.ready.record(a.stream)
+            return ("continue", None)
+        except (ValueError, RuntimeError, TypeError) as e:  # e.g. a non positive-definite overlap
+            return ("failed", _describe(e))
+
+    def _complete(self, a: _Active, stats, now_fn) -> None:
+        """Finish a request (finisher thread, on the request's stream): FP64
+        refinement of a mixed solve, the final residual
+        max_b ||H psi_b - eps_b psi_b|| (one more H.psi), result checks, latency."""
+        req = a.req
+        try:
+            with torch.cuda.stream(a.stream):
+                self._finish_solve(a, stats)
         except (ValueError, RuntimeError) as e:
-            req.status, req.error = "failed", str(e)
+            req.status, req.error = "failed", _describe(e)
         req.t_done = now_fn()
-        self._release(a)
+
+    def _finish_solve(self, a: _Active, stats) -> None:
+        req, el = a.req, a.el
+        converged, iterations, why = bool(stats.converged), stats.iterations, ""
+        if not converged:
+            why = f"not converged in {stats.iterations} iterations (deig_max {stats.deig_max:.2e})"
+        if self.refine:
+            # A mixed solve that stopped at FP32's floor (stalled) is finished
+            # by the FP64 sweeps.
+            inst64 = Instance(req.spec, self.device, dtype=torch.complex128)
+            el64 = inst64.electrons(req.n_bands)
+            refine_fp64(el, el64, eig_threshold=self.refine_threshold, residual_threshold=self.residual_threshold,
+                        max_sweeps=max(40, self.max_iterations - stats.iterations))
+            ref = el64.last_refine
+            req.hpsi_bands += ref.hpsi_bands
+            iterations += ref.iterations
+            converged = (converged or stats.stalled) and ref.converged
+            if not converged:
+                why = why or f"FP64 refinement not converged in {ref.iterations} sweeps (deig_max {ref.deig_max:.2e})"
+            el = el64
+        HC = el.hamiltonian(el.C)
+        res = (HC - el.C * el.eig[..., None].to(el.C.coeff.real.dtype)).band_norm()
+        req.residual = float(res[:, : req.n_bands].max())
+        eig = el.eig[:, : req.n_bands].detach().cpu().numpy()
+        if not np.all(np.isfinite(eig)):
+            raise RuntimeError("non-finite eigenvalues")
+        req.eig, req.iterations, req.converged = eig, iterations, converged
+        req.hpsi_bands += stats.hpsi_bands + el.C.n_bands() * el.basis.nk
+        req.status = "done" if converged else "failed"
+        req.error = "" if converged else why
 
     def _fail(self, a: _Active, why: str, now: float) -> None:
         a.req.status, a.req.error, a.req.t_done = "failed", why, now
         self._release(a)
 
     def _release(self, a: _Active) -> None:
+        a.stream.synchronize()
         self.active.remove(a)
         self.in_use -= a.nbytes
         self.finished.append(a.req)
@@ -267,24 +376,24 @@ class EigenServer:
         def now() -> float:
             return time.perf_counter() - t0
 
-        while self.queue or self.active:
+        while self.queue or self.active or self._completing:
+            self._reap()
             t = now()
             self._admit(t if realtime else math.inf, t)
             if not self.active:
-                if not self.queue:
+                if not self.queue and not self._completing:
                     break
-                wait = self.queue[0].arrival - now()
-                if wait > 0:
-                    time.sleep(min(wait, 0.01))
+                wait = (self.queue[0].arrival - now()) if self.queue else 0.0
+                time.sleep(min(max(wait, 0.001), 0.01))  # next arrival, or memory held by finishing requests
                 continue
             self.tick(now)
-            torch.cuda.synchronize()
             if now() > max_wall_s:
                 for a in list(self.active):
                     self._fail(a, "server time limit", now())
                 for r in self.queue:
                     self._reject(r, "server time limit", now())
                 self.queue.clear()
+        self._reap(wait=True)
         return self.report(now())
 
     def report(self, wall: float) -> dict:
@@ -298,7 +407,22 @@ class EigenServer:
                     eigensolves_per_s=len(done) / max(last - first, 1e-9), wall_s=wall,
                     p50_latency_s=float(np.percentile(lat, 50)), p99_latency_s=float(np.percentile(lat, 99)),
                     ticks=self.ticks, mean_band_apps_per_tick=float(np.mean(self.tick_band_apps)) if self.ticks else 0.0,
-                    hpsi_band_apps=int(sum(r.hpsi_bands for r in done)))
+                    hpsi_band_apps=int(sum(r.hpsi_bands for r in done)),
+                    tick_wall_s=float(sum(self.tick_wall)),
+                    hpsi_gpu_s=self.hpsi_gpu_seconds())
+
+    def hpsi_gpu_seconds(self) -> float:
+        """Device time of the batched H.psi launches (CUDA events on the server's
+        stream; the start event may also wait for the requests' blocks)."""
+        torch.cuda.synchronize(self.device)
+        return float(sum(a.elapsed_time(b) for a, b in self._hpsi_events)) * 1e-3
+
+
+def _describe(e: Exception) -> str:
+    """Error text with the innermost source location it came from."""
+    tb = traceback.extract_tb(e.__traceback__)
+    where = f" [{tb[-1].filename.rsplit('/', 1)[-1]}:{tb[-1].lineno} {tb[-1].name}]" if tb else ""
+    return f"{type(e).__name__}: {e}{where}"
 
 
 def poisson_stream(specs: list, rate_hz: float, seed: int, bands_choices=(8, 16, 32, 64, 96, 128, 160)) -> list:
