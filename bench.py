@@ -54,8 +54,8 @@ def parse_args():
     ap.add_argument("--forms", default="fp64,mixed", help="precision forms to run (profiling aid)")
     ap.add_argument("--plane-budget-mb", type=int, default=0, help="slab-plane workspace cap (0 = default)")
     ap.add_argument("--batch", type=int, default=256, help="instances of the batched workload (0 = skip)")
-    ap.add_argument("--serve", type=int, default=120, help="requests of the serving stream sample (0 = skip)")
-    ap.add_argument("--serve-wall", type=float, default=240.0, help="wall-clock cap per serving run (s)")
+    ap.add_argument("--serve", type=int, default=32, help="requests of the serving stream sample (0 = skip)")
+    ap.add_argument("--serve-wall", type=float, default=150.0, help="wall-clock cap per serving run (s)")
     ap.add_argument("--no-eigensolve", action="store_true")
     return ap.parse_args()
 
@@ -103,56 +103,101 @@ def dist_barrier(ws: int):
 
 
 class ClockSampler:
-    """nvidia-smi sampled every 200 ms in a background process."""
+    """SM clock, power and clock-event reasons sampled every millisecond through
+    NVML (read-only queries) in a background thread, so that even a timed region
+    of a few tens of milliseconds gets samples.  Falls back to `nvidia-smi -lms`
+    where NVML cannot be loaded."""
 
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, index: int):
         self.index = index
-        self.proc = None
-        self.lines: list[str] = []
+        self.samples: list = []
+        self._stop = threading.Event()
+        self._nvml = None
+        self._handle = None
+        self._smi = None
+
+    def _open_nvml(self):
+        import torch
+
+        lib = ct.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = ct.c_void_p()
+        props = torch.cuda.get_device_properties(self.index)
+        bus = None
+        if all(hasattr(props, a) for a in ("pci_domain_id", "pci_bus_id", "pci_device_id")):
+            bus = f"{props.pci_domain_id:08x}:{props.pci_bus_id:02x}:{props.pci_device_id:02x}.0"
+        if bus is None or lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ct.byref(h)) != 0:
+            if lib.nvmlDeviceGetHandleByIndex_v2(self.index, ct.byref(h)) != 0:
+                raise OSError("no NVML handle")
+        self._nvml, self._handle = lib, h
+        self._reasons_fn = None
+        for name in ("nvmlDeviceGetCurrentClocksEventReasons", "nvmlDeviceGetCurrentClocksThrottleReasons"):
+            try:
+                self._reasons_fn = getattr(lib, name)
+                break
+            except AttributeError:
+                continue
+
+    def _sample_nvml(self):
+        lib, h = self._nvml, self._handle
+        sm, smax, pw, rs = ct.c_uint(), ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        while not self._stop.is_set():
+            ok = lib.nvmlDeviceGetClockInfo(h, 1, ct.byref(sm)) == 0  # NVML_CLOCK_SM
+            lib.nvmlDeviceGetMaxClockInfo(h, 1, ct.byref(smax))
+            lib.nvmlDeviceGetPowerUsage(h, ct.byref(pw))
+            if self._reasons_fn is not None:
+                self._reasons_fn(h, ct.byref(rs))
+            if ok:
+                self.samples.append((sm.value, smax.value, pw.value / 1000.0, rs.value))
+            time.sleep(0.001)
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self._t = threading.Thread(target=self._read, daemon=True)
+            self._open_nvml()
+            self._t = threading.Thread(target=self._sample_nvml, daemon=True)
             self._t.start()
-        except OSError:
-            self.proc = None
+        except (OSError, AttributeError):
+            self._nvml = None
+            try:
+                self._smi = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,power.draw",
+                     "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                    stderr=subprocess.DEVNULL, text=True)
+                self._t = threading.Thread(target=self._read_smi, daemon=True)
+                self._t.start()
+            except OSError:
+                self._smi = None
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    def _read_smi(self):
+        for line in self._smi.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            try:
+                self.samples.append((float(parts[0]), float(parts[1]), float(parts[2]), 0))
+            except (ValueError, IndexError):
+                continue
 
     def stop(self) -> dict:
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 7:
-                continue
+        self._stop.set()
+        if self._smi is not None:
+            self._smi.terminate()
             try:
-                sm.append(float(parts[0]))
-                smax.append(float(parts[1]))
-            except ValueError:
-                continue
-            for name, v in zip(names, parts[3:7]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": float(max(smax)) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                self._smi.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._smi.kill()
+        if getattr(self, "_t", None) is not None:
+            self._t.join(timeout=5)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no clock samples"], "samples": 0}
+        sm = [x[0] for x in self.samples]
+        reasons = sorted({name for x in self.samples for bit, name in self.REASONS.items() if x[3] & bit})
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(x[1] for x in self.samples)),
+                "sm_min_mhz": float(min(sm)), "power_w_median": float(np.median([x[2] for x in self.samples])),
+                "reasons": reasons, "samples": len(sm), "source": "nvml" if self._nvml is not None else "nvidia-smi"}
 
 
 # ---------------------------------------------------------------------------
@@ -183,6 +228,50 @@ def roofline_counts(p, b, tables, nb_tile: int, real_bytes: int):
     bytes_loc = 2 * n * s_c + (N * real_bytes + n * 4) / nb_tile
     bytes_nl = 2 * n * s_c + 2 * P * n * s_c / nb_tile
     return dict(flops_loc=flops_loc, flops_nl=flops_nl, bytes_loc=bytes_loc, bytes_nl=bytes_nl)
+
+
+# DRAM bytes (read + write) per 32-band si64 block, from one ncu capture of the
+# mixed form (`--set full`, default cache control: caches flushed before every
+# kernel, so planes one kernel writes and the next reads count as DRAM traffic
+# although they stay in L2 in a timed run).  Command and per-kernel figures:
+# profiles/ncu_local_si64_mixed.md.
+NCU_DRAM_BYTES_PER_BLOCK = {"local": 296.4e6, "nonlocal": 196.7e6}
+
+
+def local_roofline(rc, band_apps, t_loc, hbm_peak, peaks) -> dict:
+    """Roofline of the local-potential apply (three launches in one C-ABI call,
+    one 32-band block): achieved = algorithmic bytes / CUDA-event time against
+    the measured HBM copy bandwidth, with the measured DRAM traffic beside it;
+    the bound that binds is the FP32 CUDA-core pipe (5 N log2 N flops per FFT at
+    ~300 flop per compulsory byte), reported as `pipe`."""
+    ach_gbs = rc["bytes_loc"] * band_apps / t_loc / 1e9
+    ach_tflops = rc["flops_loc"] * band_apps / t_loc / 1e12
+    traffic = NCU_DRAM_BYTES_PER_BLOCK["local"]
+    t_lb = max(rc["bytes_loc"] * band_apps / (hbm_peak * 1e9), rc["flops_loc"] * band_apps / (peaks["fp32"] * 1e12))
+    return {"kernel": "local potential: k_ifft_yz + k_xpass_async + k_fft_yz_gather, one 32-band block, FP32",
+            "bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": ach_gbs / hbm_peak,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)", "traffic": traffic,
+            "dram_gbs_from_traffic": traffic / t_loc / 1e9 if traffic else None,
+            "binding": "fp32 CUDA-core pipe",
+            "pipe": {"achieved_tflops": ach_tflops, "peak_tflops": peaks["fp32"], "frac": ach_tflops / peaks["fp32"],
+                     "peak_source": "measured FMA burn (qgb_fma_burn)"},
+            "lower_bound_over_measured": t_lb / t_loc, "seconds_per_launch_group": t_loc}
+
+
+def nonlocal_roofline(rc, band_apps, t_nl, hbm_peak, bf16_peak) -> dict:
+    """Tensor-core nonlocal chain (split, <beta|psi> GEMM, reduce, D, back-projection
+    GEMM) for one 32-band block: algorithmic complex flops (2 * 8 P n per band)
+    against the bf16 tensor peak, counting the 3 bf16 products of split-BF16x3
+    and the 4 real products of a complex MAC as issued MMA work."""
+    flops = rc["flops_nl"] * band_apps
+    issued = 3.0 * flops  # split-BF16x3: hi*hi + hi*lo + lo*hi
+    traffic = NCU_DRAM_BYTES_PER_BLOCK["nonlocal"]
+    return {"bound": "hbm" if rc["bytes_nl"] / hbm_peak > rc["flops_nl"] * 3 / (bf16_peak * 1e3) else "tensor",
+            "achieved_tflops": flops / t_nl / 1e12, "issued_mma_tflops": issued / t_nl / 1e12,
+            "peak_tflops": bf16_peak, "frac_issued": issued / t_nl / 1e12 / bf16_peak,
+            "achieved_gbs": rc["bytes_nl"] * band_apps / t_nl / 1e9, "hbm_frac": rc["bytes_nl"] * band_apps / t_nl / 1e9 / hbm_peak,
+            "traffic": traffic, "dram_gbs_from_traffic": traffic / t_nl / 1e9 if traffic else None,
+            "seconds_per_block": t_nl}
 
 
 def measure_fma_peak(dtype_code: int) -> float:
@@ -268,8 +357,7 @@ def run_gb300(args, rank, ws, local):
         torch.cuda.synchronize()
         dist_barrier(ws)
         clock = ClockSampler(local)
-        if form == "mixed":
-            clock.start()
+        clock.start()
         times, t_loc, t_nl = [], [], []
         for _ in range(args.steps):
             flush.zero_()
@@ -283,7 +371,7 @@ def run_gb300(args, rank, ws, local):
             for j in range(len(blocks)):
                 t_loc.append(evs[3 * j].elapsed_time(evs[3 * j + 1]) * 1e-3)
                 t_nl.append(evs[3 * j + 1].elapsed_time(evs[3 * j + 2]) * 1e-3)
-        clocks = clock.stop() if form == "mixed" else None
+        clocks = clock.stop()
         HC = torch.cat(H_blk, dim=1)
         dist_barrier(ws)
         total = dist_max(float(np.sum(times)), ws)
@@ -524,25 +612,23 @@ def main():
     import json as _j
 
     peaks_file = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    hbm_peak = _j.load(open(peaks_file))["hbm_gbs"] if os.path.exists(peaks_file) else 6800.0
-    ach_gbs = rc["bytes_loc"] * band_apps_block / t_loc / 1e9
-    ach_tflops = rc["flops_loc"] * band_apps_block / t_loc / 1e12
+    measured = _j.load(open(peaks_file)) if os.path.exists(peaks_file) else {}
+    hbm_peak = measured.get("hbm_gbs", 6800.0)
+    bf16_peak = measured.get("bf16_tflops", 1900.0)
     out = {
         "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (f32)", "data": "synthetic",
         "config": {"workload": f"{args.workload}: 64-atom Si, 96^3 grid, n=37073, Gamma, 160 bands in blocks of 32, P=256",
                    "l2": "flushed (512 MB write) between timed steps", "parallelism": f"replicas x{ws}"},
-        "fp64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"], "e2e": f64.get("e2e")},
+        "fp64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"], "e2e": f64.get("e2e"),
+                 "clocks": f64["clocks"]},
         "mixed_over_fp64": mixed["value"] / f64["value"],
         "e2e": mixed.get("e2e"),
         "stages_ms_per_block": {"mixed": {"local": 1e3 * mixed["t_loc_block"], "nonlocal": 1e3 * mixed["t_nl_block"]},
                                 "fp64": {"local": 1e3 * f64["t_loc_block"], "nonlocal": 1e3 * f64["t_nl_block"]}},
-        "roofline": {"kernel": "apply_potential (k_ifft_yz + k_xpass + k_fft_yz_gather), mixed",
-                     "bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": ach_gbs / hbm_peak, "traffic": None,
-                     "fp32": {"achieved_tflops": ach_tflops, "peak_tflops": peaks["fp32"],
-                              "frac": ach_tflops / peaks["fp32"]}},
+        "roofline": local_roofline(rc, band_apps_block, t_loc, hbm_peak, peaks),
+        "nonlocal_roofline": nonlocal_roofline(rc, band_apps_block, mixed["t_nl_block"], hbm_peak, bf16_peak),
         "measured_fma_peaks_tflops": peaks,
         "gpu_launches": mixed["launches_per_step"] * args.steps,
         "clocks": mixed["clocks"],

@@ -409,6 +409,7 @@ class EigenServer:
                     ticks=self.ticks, mean_band_apps_per_tick=float(np.mean(self.tick_band_apps)) if self.ticks else 0.0,
                     hpsi_band_apps=int(sum(r.hpsi_bands for r in done)),
                     tick_wall_s=float(sum(self.tick_wall)),
+                    errors=[f"{r.rid}: {r.error[:160]}" for r in self.finished if r.status != "done"][:8],
                     hpsi_gpu_s=self.hpsi_gpu_seconds())
 
     def hpsi_gpu_seconds(self) -> float:
