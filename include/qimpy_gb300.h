@@ -166,9 +166,12 @@ int qgb_apply_potential_static(const qgb_sphere* s, int dtype, const void* C, vo
 size_t qgb_static_scratch_bytes(void);
 
 /*
- * Shared memory per CTA the local-potential kernels need for a sphere (host).
+ * Shared memory per CTA the local-potential kernels need for a sphere (host):
+ * the largest over the three kernels (the x-phase kernel's), and that of the
+ * two y/z-phase kernels alone.
  */
 size_t qgb_sphere_smem_bytes(const qgb_sphere* s, int dtype);
+size_t qgb_sphere_smem_bytes_yz(const qgb_sphere* s, int dtype);
 
 /*
  * Batched Basis.apply_potential (qimpy/dft/electrons/_basis_ops.py:39-113) for
@@ -177,13 +180,14 @@ size_t qgb_sphere_smem_bytes(const qgb_sphere* s, int dtype);
  * problems' band blocks; `slab_starts` and `row_starts` (device, n_items + 1
  * prefix sums) give each item's work units: nk * nb * max_slabs for the y/z
  * phases and nk * nb * N1 for the x phase; `slab_item` / `row_item` (device,
- * one int per unit) name the item of every unit; smem_bytes = max over items
- * of qgb_sphere_smem_bytes.  Launch-only (capturable in a CUDA graph).
+ * one int per unit) name the item of every unit; smem_yz / smem_x = max over
+ * items of qgb_sphere_smem_bytes_yz / qgb_sphere_smem_bytes.  Launch-only
+ * (capturable in a CUDA graph).
  */
 int qgb_apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,
                                 const long long* slab_starts, const int* row_item, const long long* row_starts,
-                                long long n_slab_units, long long n_row_units, int dtype, size_t smem_bytes,
-                                void* stream);
+                                long long n_slab_units, long long n_row_units, int dtype, size_t smem_yz,
+                                size_t smem_x, void* stream);
 
 /*
  * projT[k][b][p] = sum_g conj(beta[k][p][g]) C[k][b][g]  (replaces Wavefunction.proj

@@ -69,9 +69,10 @@ _SIGS = {
                                               ct.c_uint, ct.c_void_p]),
     "qgb_static_scratch_bytes": (ct.c_size_t, []),
     "qgb_sphere_smem_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int]),
+    "qgb_sphere_smem_bytes_yz": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int]),
     "qgb_apply_potential_batched": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                                ct.c_void_p, ct.c_longlong, ct.c_longlong, ct.c_int, ct.c_size_t,
-                                               ct.c_void_p]),
+                                               ct.c_size_t, ct.c_void_p]),
     "qgb_beta_split_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int]),
     "qgb_beta_split": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
     "qgb_nonlocal_tc_workspace_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int, ct.c_int]),

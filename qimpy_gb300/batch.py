@@ -226,7 +226,7 @@ class _Group:
         offs = np.concatenate(([0], np.cumsum([(b + 255) // 256 * 256 for b in per])))
         self._planes = torch.empty(int(offs[-1]), dtype=torch.uint8, device=device)
         items = (_lib.QgbBatchItem * n)()
-        slab_units, row_units, smem = [0], [0], 0
+        slab_units, row_units, smem, smem_yz = [0], [0], 0, 0
         for i, inst in enumerate(instances):
             t = inst.tables
             items[i].sphere = self._spheres.data_ptr() + i * ssz
@@ -238,13 +238,15 @@ class _Group:
             slab_units.append(slab_units[-1] + t.nk * inst.nb * t.max_slabs)
             row_units.append(row_units[-1] + t.nk * inst.nb * t.shape[1])
             smem = max(smem, int(lib.qgb_sphere_smem_bytes(ct.byref(inst.sphere.struct), _lib.QGB_F32)))
+            smem_yz = max(smem_yz, int(lib.qgb_sphere_smem_bytes_yz(ct.byref(inst.sphere.struct), _lib.QGB_F32)))
         self._items = torch.frombuffer(bytearray(bytes(items)), dtype=torch.uint8).to(device)
         self._slab_starts = torch.tensor(slab_units, dtype=torch.int64, device=device)
         self._row_starts = torch.tensor(row_units, dtype=torch.int64, device=device)
         ids = np.arange(n, dtype=np.int32)
         self._slab_item = torch.from_numpy(np.repeat(ids, np.diff(slab_units))).to(device)
         self._row_item = torch.from_numpy(np.repeat(ids, np.diff(row_units))).to(device)
-        self.n_slab_units, self.n_row_units, self.smem = slab_units[-1], row_units[-1], smem
+        self.n_slab_units, self.n_row_units = slab_units[-1], row_units[-1]
+        self.smem, self.smem_yz = smem, smem_yz
         self._nl_ws = [ops.workspace(int(lib.qgb_nonlocal_tc_workspace_bytes(i.nk, i.beta.shape[1], i.nb, i.n_tot)),
                                      device) for i in instances]
         self._projT = [torch.empty((i.nk, i.nb, i.beta.shape[1]), dtype=torch.complex64, device=device)
@@ -256,7 +258,7 @@ class _Group:
                                                            self._slab_item.data_ptr(), self._slab_starts.data_ptr(),
                                                            self._row_item.data_ptr(), self._row_starts.data_ptr(),
                                                            self.n_slab_units, self.n_row_units, _lib.QGB_F32,
-                                                           self.smem, st), "apply_potential_batched")
+                                                           self.smem_yz, self.smem, st), "apply_potential_batched")
         for i, inst in enumerate(self.instances):
             ops.apply_nonlocal_tc(inst.split, inst.D, self.inputs[i], self.outputs[i], self._projT[i], self._nl_ws[i])
 

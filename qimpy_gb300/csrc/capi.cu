@@ -41,9 +41,11 @@ int apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int 
 int debug_violation(unsigned long long* out4);
 #endif
 size_t sphere_smem_bytes(const qgb_sphere& s, int dtype);
+size_t plane_smem_bytes(const qgb_sphere& s, int dtype);
 int apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,
                             const long long* slab_starts, const int* row_item, const long long* row_starts,
-                            long long n_slab, long long n_row, int dtype, size_t smem, cudaStream_t st);
+                            long long n_slab, long long n_row, int dtype, size_t smem_yz, size_t smem_x,
+                            cudaStream_t st);
 size_t beta_split_bytes(int nk, int P, int n_tot);
 int beta_split(const void* beta, int nk, int P, int n_tot, void* out, size_t out_bytes, cudaStream_t st);
 size_t nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot);
@@ -138,13 +140,14 @@ int qgb_debug_violation(unsigned long long* out4) { return qgb::debug_violation(
 #endif
 
 size_t qgb_sphere_smem_bytes(const qgb_sphere* s, int dtype) { return s ? sphere_smem_bytes(*s, dtype) : 0; }
+size_t qgb_sphere_smem_bytes_yz(const qgb_sphere* s, int dtype) { return s ? plane_smem_bytes(*s, dtype) : 0; }
 
 int qgb_apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,
                                 const long long* slab_starts, const int* row_item, const long long* row_starts,
-                                long long n_slab_units, long long n_row_units, int dtype, size_t smem_bytes,
-                                void* stream) {
+                                long long n_slab_units, long long n_row_units, int dtype, size_t smem_yz,
+                                size_t smem_x, void* stream) {
   return apply_potential_batched(items, n_items, slab_item, slab_starts, row_item, row_starts, n_slab_units,
-                                 n_row_units, dtype, smem_bytes, static_cast<cudaStream_t>(stream));
+                                 n_row_units, dtype, smem_yz, smem_x, static_cast<cudaStream_t>(stream));
 }
 
 size_t qgb_beta_split_bytes(int nk, int P, int n_tot) { return beta_split_bytes(nk, P, n_tot); }

@@ -279,9 +279,9 @@ __device__ __forceinline__ void xmid_dispatch(int L1, cplx_t<T>* sm, int p, int 
 template <typename T>
 __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const LocalParams& lp,
                                                  cplx_t<T>* __restrict__ planes, const int r1, const int b,
-                                                 const int k) {
+                                                 const int k, const int z0, const int nz) {
   using C2 = cplx_t<T>;
-  const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 2;
+  const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = nz + 2;
   const int L1 = s.L1[0], L2 = s.L2[0];
   const int lim = N0 * ld, Wx = lim;
   C2* sm = smem_c<T>();
@@ -291,50 +291,50 @@ __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const Loca
   const C2 zero = mk<T>(T(0), T(0));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int r = warp; r < N0; r += nwarps)
-    for (int c = lane; c < N2; c += 32) sm[r * ld + c] = zero;
+    for (int c = lane; c < nz; c += 32) sm[r * ld + c] = zero;
   __syncthreads();
 
   const int nslabs = s.n_slabs[k];
   const int* i0 = s.slab_i0 + k * s.max_slabs;
   const size_t plane = static_cast<size_t>(N1) * N2;
-  C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2;
-  // Group 1: slab rows (16 B = 2 complex per copy).
-  const int cpr = N2 / 2;  // copies per row
+  C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2 + z0;
+  // Group 1: slab rows, columns [z0, z0 + nz) (16 B = 2 complex per copy).
+  const int cpr = nz / 2;  // copies per row
   for (int it = threadIdx.x; it < nslabs * cpr; it += blockDim.x) {
     const int sl = it / cpr, c = 2 * (it - sl * cpr);
     cp_async16(sm + i0[sl] * ld + c, base + sl * plane + c);
   }
   cp_async_commit();
-  // Group 2: V slice V[p0][r1][*] for all p0 (16 B = 4 reals per copy).
+  // Group 2: V slice V[p0][r1][z0 .. z0 + nz) for all p0 (16 B = 4 reals per copy).
   const T* V = static_cast<const T*>(s.V);
-  const int vpr = N2 / 4;
+  const int vpr = nz / 4;
   for (int it = threadIdx.x; it < N0 * vpr; it += blockDim.x) {
     const int p0 = it / vpr, c = 4 * (it - p0 * vpr);
-    cp_async16(Vs + p0 * N2 + c, V + (static_cast<size_t>(p0) * N1 + r1) * N2 + c);
+    cp_async16(Vs + p0 * nz + c, V + (static_cast<size_t>(p0) * N1 + r1) * N2 + z0 + c);
   }
   cp_async_commit();
   cp_async_wait<1>();
   __syncthreads();
 
   if (L2 > 1) {
-    run_pass<T, +1>(L2, Pass{nullptr, 0, N2, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
+    run_pass<T, +1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
   }
   cp_async_wait<0>();
   __syncthreads();
-  for (int it = threadIdx.x; it < N2 * L2; it += blockDim.x) {
-    const int a = it / N2;
-    const int c = it - a * N2;
-    xmid_dispatch<T>(L1, sm, c + a * L1 * ld, ld, Vs + a * L1 * N2 + c, static_cast<size_t>(N2), Wx, L2, a);
+  for (int it = threadIdx.x; it < nz * L2; it += blockDim.x) {
+    const int a = it / nz;
+    const int c = it - a * nz;
+    xmid_dispatch<T>(L1, sm, c + a * L1 * ld, ld, Vs + a * L1 * nz + c, static_cast<size_t>(nz), Wx, L2, a);
   }
   __syncthreads();
   if (L2 > 1) {
-    run_pass<T, -1>(L2, Pass{nullptr, 0, N2, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
+    run_pass<T, -1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
     __syncthreads();
   }
   for (int sl = warp; sl < nslabs; sl += nwarps) {
     C2* dst = base + sl * plane;
     const int x = i0[sl];
-    for (int c = lane; c < N2; c += 32) dst[c] = sm[x * ld + c];
+    for (int c = lane; c < nz; c += 32) dst[c] = sm[x * ld + c];
   }
 }
 
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_xpass_async(const qgb_sphere s, LocalParams lp,
                                                           cplx_t<T>* __restrict__ planes) {
-  body_xpass_async<T>(s, lp, planes, blockIdx.x, blockIdx.y, blockIdx.z);
+  body_xpass_async<T>(s, lp, planes, blockIdx.x, blockIdx.y, blockIdx.z, 0, s.N[2]);
 }
 
 // C and out may alias (in-place apply): no __restrict__ on them.
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(kThreads) k_xpass_batched(const qgb_batch_item
   const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
   const int b = static_cast<int>(rest % ctx.it.nb), k = static_cast<int>(rest / ctx.it.nb);
   if (sizeof(T) == 4 && s.N[2] % 4 == 0)
-    body_xpass_async<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k);
+    body_xpass_async<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k, 0, s.N[2]);
   else
     body_xpass<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k);
 }
@@ -585,6 +585,19 @@ size_t plane_bytes_per_band(const qgb_sphere& s, int dtype) {
   return static_cast<size_t>(s.nk) * s.max_slabs * s.N[1] * s.N[2] * elem_bytes(dtype);
 }
 
+static int launch_xpass_async(const qgb_sphere& s, const LocalParams& lp, float2* planes, cudaStream_t st) {
+  static size_t configured = 0;
+  const size_t smx = xpass_async_smem_bytes(s);
+  if (smx > configured) {
+    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_async<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
+    configured = smx;
+  }
+  const dim3 g2(s.N[1], lp.nb, s.nk);
+  k_xpass_async<float><<<g2, kThreads, smx, st>>>(s, lp, planes);
+  QGB_LAUNCH_CHECK("k_xpass_async");
+  return QGB_OK;
+}
+
 template <typename T>
 static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* C, void* out,
                         void* planes, cudaStream_t st, size_t smem) {
@@ -592,17 +605,11 @@ static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* 
   const dim3 g1(s.max_slabs, lp.nb, s.nk);
   k_ifft_yz<T><<<g1, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(C), static_cast<C2*>(planes));
   QGB_LAUNCH_CHECK("k_ifft_yz");
-  const dim3 g2(s.N[1], lp.nb, s.nk);
   if (sizeof(T) == 4 && s.N[2] % 4 == 0) {
-    const size_t smx = xpass_async_smem_bytes(s);
-    static size_t configured = 0;
-    if (smx > configured) {
-      QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_async<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
-      configured = smx;
-    }
-    k_xpass_async<T><<<g2, kThreads, smx, st>>>(s, lp, static_cast<C2*>(planes));
-    QGB_LAUNCH_CHECK("k_xpass_async");
+    const int rc = launch_xpass_async(s, lp, static_cast<float2*>(planes), st);
+    if (rc) return rc;
   } else {
+    const dim3 g2(s.N[1], lp.nb, s.nk);
     k_xpass<T><<<g2, kThreads, smem, st>>>(s, lp, static_cast<C2*>(planes));
     QGB_LAUNCH_CHECK("k_xpass");
   }
@@ -654,39 +661,52 @@ size_t sphere_smem_bytes(const qgb_sphere& s, int dtype) {
   return smem;
 }
 
+// The y/z kernels get the y/z-phase shared memory and the x kernel its own
+// (larger for the asynchronous FP32 x-pass, which also stages V): giving all
+// three the largest size would cost the y/z kernels a CTA per SM.
 template <typename T>
 static int launch_batched(const qgb_batch_item* items, const int* slab_item, const long long* slab_starts,
                           const int* row_item, const long long* row_starts, long long n_slab, long long n_row,
-                          size_t smem, cudaStream_t st) {
-  static size_t configured = 0;
-  if (smem > configured) {
-    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                          size_t smem_yz, size_t smem_x, cudaStream_t st) {
+  static size_t configured_yz = 0, configured_x = 0;
+  if (smem_yz > configured_yz) {
+    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem_yz));
     QGB_CUDA_CHECK(cudaFuncSetAttribute(k_fft_yz_gather_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-    configured = smem;
+                                        (int)smem_yz));
+    configured_yz = smem_yz;
   }
-  k_ifft_yz_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_item, slab_starts);
+  if (smem_x > configured_x) {
+    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem_x));
+    configured_x = smem_x;
+  }
+  k_ifft_yz_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem_yz, st>>>(items, slab_item, slab_starts);
   QGB_LAUNCH_CHECK("k_ifft_yz_batched");
-  k_xpass_batched<T><<<static_cast<unsigned>(n_row), kThreads, smem, st>>>(items, row_item, row_starts);
+  k_xpass_batched<T><<<static_cast<unsigned>(n_row), kThreads, smem_x, st>>>(items, row_item, row_starts);
   QGB_LAUNCH_CHECK("k_xpass_batched");
-  k_fft_yz_gather_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem, st>>>(items, slab_item, slab_starts);
+  k_fft_yz_gather_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem_yz, st>>>(items, slab_item,
+                                                                                        slab_starts);
   QGB_LAUNCH_CHECK("k_fft_yz_gather_batched");
   return QGB_OK;
 }
 
 int apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,
                             const long long* slab_starts, const int* row_item, const long long* row_starts,
-                            long long n_slab, long long n_row, int dtype, size_t smem, cudaStream_t st) {
+                            long long n_slab, long long n_row, int dtype, size_t smem_yz, size_t smem_x,
+                            cudaStream_t st) {
   if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
   if (n_items < 0 || n_slab < 0 || n_row < 0) return fail(QGB_ERR_INVALID, "negative batch sizes");
   if (n_items == 0 || n_slab == 0) return QGB_OK;
   if (!items || !slab_starts || !row_starts || !slab_item || !row_item) return fail(QGB_ERR_INVALID, "NULL batch table");
   if (n_slab > 0x7FFFFFFFLL || n_row > 0x7FFFFFFFLL) return fail(QGB_ERR_UNSUPPORTED, "batch too large for one grid");
-  if (smem > 227 * 1024) return fail(QGB_ERR_UNSUPPORTED, "batched shared memory %zu B > 227 KB", smem);
-  return dtype == QGB_F64
-             ? launch_batched<double>(items, slab_item, slab_starts, row_item, row_starts, n_slab, n_row, smem, st)
-             : launch_batched<float>(items, slab_item, slab_starts, row_item, row_starts, n_slab, n_row, smem, st);
+  if (smem_yz > 227 * 1024 || smem_x > 227 * 1024)
+    return fail(QGB_ERR_UNSUPPORTED, "batched shared memory %zu / %zu B > 227 KB", smem_yz, smem_x);
+  if (smem_x < smem_yz) return fail(QGB_ERR_INVALID, "smem_x %zu < smem_yz %zu", smem_x, smem_yz);
+  return dtype == QGB_F64 ? launch_batched<double>(items, slab_item, slab_starts, row_item, row_starts, n_slab, n_row,
+                                                   smem_yz, smem_x, st)
+                          : launch_batched<float>(items, slab_item, slab_starts, row_item, row_starts, n_slab, n_row,
+                                                  smem_yz, smem_x, st);
 }
 
 int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, cudaStream_t st) {

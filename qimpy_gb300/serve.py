@@ -222,7 +222,7 @@ class EigenServer:
         st = torch.cuda.current_stream().cuda_stream
         for idx in groups.values():
             items = (_lib.QgbBatchItem * len(idx))()
-            slab_units, row_units, smem = [0], [0], 0
+            slab_units, row_units, smem, smem_yz = [0], [0], 0, 0
             for j, i in enumerate(idx):
                 a = acts[i]
                 t = a.inst.tables
@@ -236,6 +236,7 @@ class EigenServer:
                 slab_units.append(slab_units[-1] + t.nk * nb * t.max_slabs)
                 row_units.append(row_units[-1] + t.nk * nb * t.shape[1])
                 smem = max(smem, int(lib.qgb_sphere_smem_bytes(ct.byref(a.inst.sphere.struct), self.qdtype)))
+                smem_yz = max(smem_yz, int(lib.qgb_sphere_smem_bytes_yz(ct.byref(a.inst.sphere.struct), self.qdtype)))
             ids = np.arange(len(idx), dtype=np.int32)
             dev_items = torch.frombuffer(bytearray(bytes(items)), dtype=torch.uint8).to(self.device)
             starts_s = torch.tensor(slab_units, dtype=torch.int64, device=self.device)
@@ -244,7 +245,7 @@ class EigenServer:
             item_r = torch.from_numpy(np.repeat(ids, np.diff(row_units))).to(self.device)
             _lib.check(lib.qgb_apply_potential_batched(dev_items.data_ptr(), len(idx), item_s.data_ptr(),
                                                        starts_s.data_ptr(), item_r.data_ptr(), starts_r.data_ptr(),
-                                                       slab_units[-1], row_units[-1], self.qdtype, smem, st),
+                                                       slab_units[-1], row_units[-1], self.qdtype, smem_yz, smem, st),
                        "apply_potential_batched")
             for i in idx:
                 a, C = acts[i], acts[i].block.coeff
