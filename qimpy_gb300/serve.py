@@ -75,10 +75,12 @@ class EigenServer:
 
     def __init__(self, device="cuda", precision: str = "mixed", hbm_budget_bytes: int = 160 << 30,
                  max_active: int = 64, eig_threshold: float = 1e-6, residual_threshold: Optional[float] = None,
-                 max_iterations: int = 200, refine: bool = True, refine_threshold: float = 1e-8,
+                 max_iterations: int = 200, refine: bool = True, refine_threshold: Optional[float] = None,
                  workers: int = 16):
         """eig_threshold: Davidson's stop on the largest eigenvalue change (Ha);
-        refine_threshold: the same for the FP64 refinement of a mixed solve;
+        refine_threshold: the same for the FP64 refinement of a mixed solve
+        (default eig_threshold / 10); a refinement that ends
+        above it but within eig_threshold still completes the request;
         residual_threshold: optional extra stop on the FP64 residual norm
         (FP64 solve, or the refinement).  Every finished request reports its
         final residual."""
@@ -94,7 +96,7 @@ class EigenServer:
         self.residual_threshold = residual_threshold
         self.max_iterations = max_iterations
         self.refine = refine and precision == "mixed"
-        self.refine_threshold = refine_threshold
+        self.refine_threshold = refine_threshold if refine_threshold is not None else eig_threshold / 10
         self.queue: list = []
         self.active: list = []
         self.finished: list = []
@@ -108,7 +110,7 @@ class EigenServer:
         self._pool = ThreadPoolExecutor(max_workers=workers)
         # Finished solves (FP64 refinement, final residual) complete beside the
         # next ticks on a pool of their own.
-        self._finisher = ThreadPoolExecutor(max_workers=max(1, workers // 4))
+        self._finisher = ThreadPoolExecutor(max_workers=max(1, workers // 2))
         self._completing: list = []
         self._warm_up()
         self.tick_wall: list = []  #: host seconds per tick
@@ -339,7 +341,7 @@ class EigenServer:
             ref = el64.last_refine
             req.hpsi_bands += ref.hpsi_bands
             iterations += ref.iterations
-            converged = (converged or stats.stalled) and ref.converged
+            converged = (converged or stats.stalled) and (ref.converged or ref.deig_max <= self.eig_threshold)
             if not converged:
                 why = why or f"FP64 refinement not converged in {ref.iterations} sweeps (deig_max {ref.deig_max:.2e})"
             el = el64
