@@ -74,20 +74,30 @@ def dist_init():
     if ws > 1:
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        backend = os.environ.get("QGB_DIST_BACKEND", "nccl")  # gloo: CPU tests of the replica plumbing
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return rank, ws, local
 
 
 def dist_max(x: float, ws: int) -> float:
+    """Maximum of a host scalar over ranks (the slowest replica's time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(units_per_rank: float, max_seconds: float, ws: int) -> float:
+    """Whole-job throughput of `ws` independent replicas: the units of all ranks
+    over the max-over-ranks time (from dist_max)."""
+    return units_per_rank * ws / max_seconds
 
 
 def dist_barrier(ws: int):
@@ -375,7 +385,7 @@ def run_gb300(args, rank, ws, local):
         HC = torch.cat(H_blk, dim=1)
         dist_barrier(ws)
         total = dist_max(float(np.sum(times)), ws)
-        res = dict(value=nb * p.nk * args.steps * ws / total, ms_per_step=1e3 * total / args.steps,
+        res = dict(value=replica_value(nb * p.nk * args.steps, total, ws), ms_per_step=1e3 * total / args.steps,
                    t_loc_block=float(np.median(t_loc)), t_nl_block=float(np.median(t_nl)),
                    clocks=clocks)
         # End-to-end through the public API with host buffers (pinned), every step.
@@ -404,7 +414,7 @@ def run_gb300(args, rank, ws, local):
                 e2e_times.append(e0.elapsed_time(e1) * 1e-3)
             tot = dist_max(float(np.sum(e2e_times)), ws)
             nbytes = Ch.numel() * Ch.element_size()
-            res["e2e"] = dict(value=nb * p.nk * args.steps * ws / tot, unit=UNIT, h2d_bytes_per_step=nbytes,
+            res["e2e"] = dict(value=replica_value(nb * p.nk * args.steps, tot, ws), unit=UNIT, h2d_bytes_per_step=nbytes,
                               d2h_bytes_per_step=nbytes)
             err = float((Hh.to(dev) - HC).abs().max() / HC.abs().max())
             res["e2e_matches_device_result"] = err
