@@ -48,6 +48,30 @@ __device__ __forceinline__ size_t plane_index(const qgb_sphere& s, int k, int b,
   return (static_cast<size_t>(k) * nb + b) * s.max_slabs + slab;
 }
 
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// One complex element global -> shared without a register round trip (8 B
+// for FP32, 16 B for FP64): many copies stay in flight per thread.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(cplx_t<T>* smem_dst, const cplx_t<T>* gsrc) {
+  if constexpr (sizeof(cplx_t<T>) == 16) {
+    cp_async16(smem_dst, gsrc);
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
+                 "l"(gsrc)
+                 : "memory");
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void body_ifft_yz(const qgb_sphere& s, const LocalParams& lp,
                                              const cplx_t<T>* __restrict__ C, cplx_t<T>* __restrict__ planes,
@@ -76,8 +100,10 @@ __device__ __forceinline__ void body_ifft_yz(const qgb_sphere& s, const LocalPar
     const int v = yz[g];
     const int pos = (v >> 16) * ld + (v & 0xFFFF);
     if (!QGB_OK_IDX(pos, lim, 2) || !QGB_OK_IDX(v & 0xFFFF, N2, 3)) continue;
-    sm[pos] = Cb[g];
+    cp_async_elem<T>(sm + pos, Cb + g);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
 
   // Inverse z-FFT along the rows this slab touches (row stride ld, element stride 1).
@@ -201,16 +227,6 @@ __device__ __forceinline__ void body_xpass(const qgb_sphere& s, const LocalParam
     C2* dst = base + sl * plane;
     for (int c = lane; c < N2; c += 32) dst[c] = sm[x * ld + c];
   }
-}
-
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
-               "l"(gsrc)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // The x-pass middle step on one item: inverse L1-point DFT, multiply by V,
@@ -354,14 +370,18 @@ __device__ __forceinline__ void body_fft_yz_gather(const qgb_sphere& s, const Lo
   const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
   const int lim = N1 * ld, Wy = lim, Wz = Wy + N1;
   C2* sm = smem_c<T>();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  if (!QGB_OK_IDX(plane_index(s, k, b, lp.nb, slab), (long long)s.nk * lp.nb * s.max_slabs, 4)) return;
+  // Stage the plane asynchronously (padded rows are 8-byte aligned only, so one
+  // element per copy), then the twiddles while the copies are in flight.
+  const C2* in = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
+  for (int r = warp; r < N1; r += nwarps)
+    for (int c = lane; c < N2; c += 32) cp_async_elem<T>(sm + r * ld + c, in + r * N2 + c);
+  cp_async_commit();
   const C2* tw = static_cast<const C2*>(s.twiddle);
   load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
   load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  if (!QGB_OK_IDX(plane_index(s, k, b, lp.nb, slab), (long long)s.nk * lp.nb * s.max_slabs, 4)) return;
-  const C2* in = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
-  for (int r = warp; r < N1; r += nwarps)
-    for (int c = lane; c < N2; c += 32) sm[r * ld + c] = in[r * N2 + c];
+  cp_async_wait<0>();
   __syncthreads();
 
   fft_forward<T>(0, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy, lim);
