@@ -277,19 +277,24 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll 1
       for (int c0 = 0; c0 < HB; c0 += 32) {
         float vr[32], vi[32];
+        // All 32 loads of HC first, then the stores: interleaved read-modify-
+        // writes through one pointer could alias, which would serialise 32
+        // memory round trips per thread.
+        float2 o[32];
+        if (row_ok) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const int b = n_tile * HB + c0 + i;
+            o[i] = b < args.nb ? hc[static_cast<long long>(b) * args.hc_ld] : make_float2(0.f, 0.f);
+          }
+        }
         tmem_ld32(trow + c0, vr);
         tmem_ld32(trow + HB + c0, vi);
         if (row_ok) {
 #pragma unroll
           for (int i = 0; i < 32; ++i) {
             const int b = n_tile * HB + c0 + i;
-            if (b < args.nb) {
-              float2* p = hc + static_cast<long long>(b) * args.hc_ld;
-              float2 o = *p;
-              o.x += vr[i];
-              o.y += vi[i];
-              *p = o;
-            }
+            if (b < args.nb) hc[static_cast<long long>(b) * args.hc_ld] = make_float2(o[i].x + vr[i], o[i].y + vi[i]);
           }
         }
       }
