@@ -2,6 +2,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <string>
+#include <unordered_map>
 
 #include "qgb_common.cuh"
 
@@ -51,6 +52,33 @@ int beta_split(const void* beta, int nk, int P, int n_tot, void* out, size_t out
 size_t nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot);
 int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
                 int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, cudaStream_t st);
+int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
+                      int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, int phases, cudaStream_t st);
+
+// A side stream and a fork/join event pair per (host thread, device): the mixed
+// Hamiltonian runs the C-only part of its nonlocal term there, beside the local
+// potential on the caller's stream (the FFT kernels are issue-bound on the CUDA
+// cores, the projector GEMMs bound by HBM and the tensor cores).  Fork and join
+// are events, so the sequence stays capturable in a CUDA graph.
+struct SideStream {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+static int side_stream(SideStream* out) {
+  static thread_local std::unordered_map<int, SideStream> streams;
+  int dev = 0;
+  QGB_CUDA_CHECK(cudaGetDevice(&dev));
+  auto it = streams.find(dev);
+  if (it == streams.end()) {
+    SideStream s;
+    QGB_CUDA_CHECK(cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking));
+    QGB_CUDA_CHECK(cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming));
+    QGB_CUDA_CHECK(cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming));
+    it = streams.emplace(dev, s).first;
+  }
+  *out = it->second;
+  return QGB_OK;
+}
 int tc_gemm_test(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N, int K,
                  int lda, int ldb, float* D, int* err, void* ws, size_t ws_bytes, cudaStream_t st);
 
@@ -184,9 +212,22 @@ int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, 
   if (workspace_bytes < nl) return fail(QGB_ERR_WORKSPACE, "workspace too small for the nonlocal term");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   char* ws = static_cast<char*>(workspace);
+  if (P == 0 || nb == 0) return apply_potential(s, QGB_F32, C, HC, nb, QGB_ADD_KE, ws + nl, workspace_bytes - nl, st);
+  SideStream f;
+  if ((rc = side_stream(&f))) return rc;
+  // Fork: the projection (split, <beta|psi>, reduce, D) on the side stream...
+  QGB_CUDA_CHECK(cudaEventRecord(f.fork, st));
+  QGB_CUDA_CHECK(cudaStreamWaitEvent(f.side, f.fork, 0));
+  const int rc_front = nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl,
+                                         dev_error, 1, f.side);
+  // ...joined back before the back-projection accumulates into HC (always, so
+  // that a capture stays well-formed even when a launch was refused).
+  QGB_CUDA_CHECK(cudaEventRecord(f.join, f.side));
   rc = apply_potential(s, QGB_F32, C, HC, nb, QGB_ADD_KE, ws + nl, workspace_bytes - nl, st);
-  if (rc || P == 0) return rc;
-  return nonlocal_tc(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl, dev_error, st);
+  QGB_CUDA_CHECK(cudaStreamWaitEvent(st, f.join, 0));
+  if (rc_front) return rc_front;
+  if (rc) return rc;
+  return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl, dev_error, 2, st);
 }
 
 int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N,

@@ -588,10 +588,12 @@ size_t nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot) {
   return static_cast<size_t>(W.partial_floats * 4 + 2 * W.psi_elems * 2 + 2 * W.b2_elems * 2) + 4 * 256 + 64;
 }
 
+// phases: 1 = steps 1-3 (everything that depends only on C), 2 = step 4 (the
+// accumulation into HC), 3 = both.  Phase 1 may run beside the local potential.
 template <int BN>
 static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC,
                             void* projT, int nk, int nb, int n_tot, const NlWorkspace& W, unsigned char* ws,
-                            int* err, cudaStream_t st) {
+                            int* err, int phases, cudaStream_t st) {
   const int P = n_atoms * pa;
   const BetaSplitLayout BL = beta_layout(nk, P, n_tot);
   auto* sbase = reinterpret_cast<const __nv_bfloat16*>(round_up(reinterpret_cast<uintptr_t>(split), 256));
@@ -606,6 +608,7 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
   auto* b2_hi = reinterpret_cast<__nv_bfloat16*>(p);
   auto* b2_lo = b2_hi + W.b2_elems;
 
+  if (phases & 1) {
   // 1. Wavefunctions -> bf16 hi/lo band rows.
   {
     dim3 grid(static_cast<unsigned>(std::min<long long>(32, (W.ldB + 255) / 256)), static_cast<unsigned>(W.rowsB), nk);
@@ -624,7 +627,7 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
   g1.part_ld = static_cast<int>(W.rowsB);
   g1.part_rows = (2LL * P + BM - 1) / BM * BM;
   g1.err = err;
-  int rc = launch<BN, kStages<BN>, EPI_PARTIAL>(
+  const int rc = launch<BN, kStages<BN>, EPI_PARTIAL>(
       Operand{a_hi, a_lo, 2LL * P, BL.ldA, 2LL * P * BL.ldA}, Operand{b_hi, b_lo, W.rowsB, W.ldB, W.rowsB * W.ldB},
       n_tot, nk, g1, st);
   if (rc) return rc;
@@ -640,6 +643,8 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
                                           static_cast<int>(W.ldB2), b2_hi, b2_lo);
     QGB_LAUNCH_CHECK("k_dapply_split");
   }
+  }
+  if (!(phases & 2)) return QGB_OK;
   // 4. HC += beta (D proj): M = basis, N = rowsB, K = 2P.
   GemmArgs g2{};
   g2.M = n_tot;
@@ -657,8 +662,8 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
       Operand{b2_hi, b2_lo, W.rowsB, W.ldB2, W.rowsB * W.ldB2}, 2 * P, nk, g2, st);
 }
 
-int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
-                int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, cudaStream_t st) {
+int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
+                      int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, int phases, cudaStream_t st) {
   const int P = n_atoms * pa;
   if (nk < 1 || nb < 0 || n_tot < 1 || P < 0) return fail(QGB_ERR_INVALID, "bad nonlocal_tc sizes");
   if (nb == 0 || P == 0) return QGB_OK;
@@ -668,10 +673,18 @@ int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const voi
   const NlWorkspace W = nl_layout(nk, P, nb, n_tot);
   unsigned char* w = static_cast<unsigned char*>(ws);
   switch (W.BN) {
-    case 64: return nonlocal_tc_impl<64>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, st);
-    case 128: return nonlocal_tc_impl<128>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, st);
-    default: return nonlocal_tc_impl<256>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, st);
+    case 64:
+      return nonlocal_tc_impl<64>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, st);
+    case 128:
+      return nonlocal_tc_impl<128>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, st);
+    default:
+      return nonlocal_tc_impl<256>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, st);
   }
+}
+
+int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
+                int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, cudaStream_t st) {
+  return nonlocal_tc_phase(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, ws, ws_bytes, err, 3, st);
 }
 
 // Plain TN GEMM for tests: D (FP32 [M][N]) = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T.

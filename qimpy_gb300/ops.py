@@ -97,7 +97,7 @@ def apply_nonlocal(beta: torch.Tensor, D_blocks: torch.Tensor, projT: torch.Tens
 
 
 def hamiltonian(sphere: DeviceSphere, C: torch.Tensor, beta: torch.Tensor | None, D_blocks: torch.Tensor | None,
-                out: torch.Tensor | None = None, projT: torch.Tensor | None = None):
+                out: torch.Tensor | None = None, projT: torch.Tensor | None = None, ws: torch.Tensor | None = None):
     """(HC, projT): HC = KE C + V C + beta D <beta|C> in one C-ABI call."""
     nb = _check_wf(sphere, C)
     out = torch.empty_like(C) if out is None else out
@@ -109,7 +109,8 @@ def hamiltonian(sphere: DeviceSphere, C: torch.Tensor, beta: torch.Tensor | None
         P = beta.shape[1]
         projT = torch.empty((C.shape[0], nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
         bptr, dptr, pptr = beta.data_ptr(), D_blocks.data_ptr(), projT.data_ptr()
-    ws = workspace(sphere.hamiltonian_workspace_bytes(nb, P), C.device)
+    if ws is None:
+        ws = workspace(sphere.hamiltonian_workspace_bytes(nb, P), C.device)
     _lib.check(_lib.lib().qgb_hamiltonian(ct.byref(sphere.struct), sphere.qdtype, C.data_ptr(), out.data_ptr(),
                                           nb, bptr, dptr, n_atoms, pa, pptr, ws.data_ptr(), ws.numel(),
                                           _stream()), "hamiltonian")
