@@ -23,6 +23,7 @@
 // Versus three full-grid passes each way this skips the empty x-planes in the
 // y/z passes and the empty z-rows in the z passes.
 #include <algorithm>
+#include <mutex>
 
 #include "fft_steps.cuh"
 
@@ -605,12 +606,22 @@ size_t plane_bytes_per_band(const qgb_sphere& s, int dtype) {
   return static_cast<size_t>(s.nk) * s.max_slabs * s.N[1] * s.N[2] * elem_bytes(dtype);
 }
 
+// Kernels' shared-memory limits are raised lazily, to the largest size asked
+// for so far; the check and the raise are one step under this lock, so that
+// host threads launching for different grids cannot lower a limit another
+// thread is about to launch with.
+static std::mutex g_attr_mu;
+
 static int launch_xpass_async(const qgb_sphere& s, const LocalParams& lp, float2* planes, cudaStream_t st) {
   static size_t configured = 0;
   const size_t smx = xpass_async_smem_bytes(s);
-  if (smx > configured) {
-    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_async<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
-    configured = smx;
+  {
+    std::lock_guard<std::mutex> lock(g_attr_mu);
+    if (smx > configured) {
+      QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_async<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smx));
+      configured = smx;
+    }
   }
   const dim3 g2(s.N[1], lp.nb, s.nk);
   k_xpass_async<float><<<g2, kThreads, smx, st>>>(s, lp, planes);
@@ -642,6 +653,7 @@ static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* 
 template <typename T>
 static int set_smem_limits(size_t smem) {
   static size_t configured = 0;
+  std::lock_guard<std::mutex> lock(g_attr_mu);
   if (smem <= configured) return QGB_OK;
   QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -689,6 +701,7 @@ static int launch_batched(const qgb_batch_item* items, const int* slab_item, con
                           const int* row_item, const long long* row_starts, long long n_slab, long long n_row,
                           size_t smem_yz, size_t smem_x, cudaStream_t st) {
   static size_t configured_yz = 0, configured_x = 0;
+  std::unique_lock<std::mutex> lock(g_attr_mu);
   if (smem_yz > configured_yz) {
     QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem_yz));
@@ -701,6 +714,7 @@ static int launch_batched(const qgb_batch_item* items, const int* slab_item, con
                                         (int)smem_x));
     configured_x = smem_x;
   }
+  lock.unlock();
   k_ifft_yz_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem_yz, st>>>(items, slab_item, slab_starts);
   QGB_LAUNCH_CHECK("k_ifft_yz_batched");
   k_xpass_batched<T><<<static_cast<unsigned>(n_row), kThreads, smem_x, st>>>(items, row_item, row_starts);

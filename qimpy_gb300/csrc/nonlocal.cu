@@ -38,13 +38,14 @@ static const char* cublas_name(cublasStatus_t s) {
       return ::qgb::fail(QGB_ERR_CUBLAS, "%s: %s", #expr, cublas_name(s_));          \
   } while (0)
 
-// One cuBLAS handle per device, created on the first nonlocal call.
+// One cuBLAS handle per (host thread, device), created on the first nonlocal
+// call of that thread.  A handle binds one stream at a time: threads sharing a
+// handle would race between cublasSetStream and the GEMM launch, putting one
+// thread's GEMM on another thread's stream.
 static int get_handle(cublasHandle_t* h) {
-  static std::mutex mu;
-  static std::unordered_map<int, cublasHandle_t> handles;
+  static thread_local std::unordered_map<int, cublasHandle_t> handles;
   int dev = 0;
   QGB_CUDA_CHECK(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(mu);
   auto it = handles.find(dev);
   if (it == handles.end()) {
     cublasHandle_t nh;
