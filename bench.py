@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--forms", default="fp64,mixed", help="precision forms to run (profiling aid)")
     ap.add_argument("--plane-budget-mb", type=int, default=0, help="slab-plane workspace cap (0 = default)")
     ap.add_argument("--batch", type=int, default=256, help="instances of the batched workload (0 = skip)")
+    ap.add_argument("--batch-chunk-mb", type=int, default=0,
+                    help="slab-plane MB per batched launch chunk (0 = one chunk per grid shape)")
     ap.add_argument("--serve", type=int, default=32, help="requests of the serving stream sample (0 = skip)")
     ap.add_argument("--serve-wall", type=float, default=150.0, help="wall-clock cap per serving run (s)")
     ap.add_argument("--no-eigensolve", action="store_true")
@@ -534,7 +536,7 @@ def run_batch(args, local):
     sched = {sh: autotune.tune_shape(sh, torch.complex64, dev) for sh in shapes}
     t_tune = time.perf_counter() - t0
     insts = [bt.Instance(s, dev, fft_factors=sched[(s.grid,) * 3]) for s in specs]
-    bh = bt.BatchedHamiltonian(insts, dev)
+    bh = bt.BatchedHamiltonian(insts, dev, plane_chunk_bytes=args.batch_chunk_mb << 20)
     bh.capture()
     t_setup = time.perf_counter() - t0
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)

@@ -238,6 +238,16 @@ size_t qgb_nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot);
 int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, int pa, const void* C, void* HC,
                           void* projT, int nk, int nb, int n_tot, void* workspace, size_t workspace_bytes,
                           int* dev_error, void* stream);
+/*
+ * The same in two phases, so that the part that reads only C can run beside
+ * the local potential (another stream): phases = 1 computes projT and the
+ * back-projection operand in `workspace` (HC untouched), phases = 2 then does
+ * HC += beta (D projT) from that workspace, phases = 3 both.  Between a
+ * phase-1 and its phase-2 call the workspace must not be reused.
+ */
+int qgb_apply_nonlocal_tc_phase(const void* beta_split, const void* D, int n_atoms, int pa, const void* C,
+                                void* HC, void* projT, int nk, int nb, int n_tot, void* workspace,
+                                size_t workspace_bytes, int* dev_error, int phases, void* stream);
 
 /*
  * Mixed-precision H C (complex64): FP32 KE + local potential (as

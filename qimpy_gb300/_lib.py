@@ -79,6 +79,9 @@ _SIGS = {
     "qgb_apply_nonlocal_tc": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
                                          ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_size_t,
                                          ct.c_void_p, ct.c_void_p]),
+    "qgb_apply_nonlocal_tc_phase": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p,
+                                               ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p,
+                                               ct.c_size_t, ct.c_void_p, ct.c_int, ct.c_void_p]),
     "qgb_hamiltonian_mixed_workspace_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int, ct.c_int]),
     "qgb_hamiltonian_mixed": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p,
                                          ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_size_t,

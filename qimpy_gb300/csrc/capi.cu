@@ -195,6 +195,14 @@ int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, in
                      dev_error, static_cast<cudaStream_t>(stream));
 }
 
+int qgb_apply_nonlocal_tc_phase(const void* beta_split, const void* D, int n_atoms, int pa, const void* C,
+                                void* HC, void* projT, int nk, int nb, int n_tot, void* workspace,
+                                size_t workspace_bytes, int* dev_error, int phases, void* stream) {
+  if (phases < 1 || phases > 3) return fail(QGB_ERR_INVALID, "phases = %d (1, 2 or 3)", phases);
+  return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, workspace, workspace_bytes,
+                           dev_error, phases, static_cast<cudaStream_t>(stream));
+}
+
 size_t qgb_hamiltonian_mixed_workspace_bytes(const qgb_sphere* s, int nb, int P) {
   if (!s || nb < 0 || P < 0) return 0;
   const size_t nl = (nonlocal_tc_workspace_bytes(s->nk, P, nb, s->n_tot) + 255) / 256 * 256;

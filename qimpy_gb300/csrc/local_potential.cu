@@ -452,75 +452,91 @@ __global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, 
 }
 
 // ... and a batch of independent spheres (cells / k-point sets / band blocks
-// with their own grids and bases) in one launch per phase.  CTA u handles the
-// work unit u of the concatenated unit ranges starts[i] <= u < starts[i + 1]
-// of item i = unit_item[u]; units are (k, band, slab) for the y/z phases and
-// (k, band, y-row) for the x phase, in that order (slab / row fastest).  The
-// item and its sphere descriptor are staged in shared memory once per CTA.
+// with their own grids and bases) in one launch per phase.  Work unit u of the
+// concatenated unit ranges starts[i] <= u < starts[i + 1] belongs to item
+// i = unit_item[u]; units are (k, band, slab) for the y/z phases and (k, band,
+// y-row) for the x phase, in that order (slab / row fastest).  Each CTA runs
+// `upc` consecutive units, so it stages an item and its sphere descriptor in
+// shared memory once for a run of units of that item rather than once per
+// unit (the three dependent loads behind it cost about as much as the FFT work
+// of one unit on the smallest grids).
 
 struct BatchCtx {
   qgb_batch_item it;
   qgb_sphere s;
-  long long local;
 };
 
-__device__ __forceinline__ void load_batch_ctx(BatchCtx& ctx, const qgb_batch_item* __restrict__ items,
-                                               const int* __restrict__ unit_item,
-                                               const long long* __restrict__ starts) {
-  if (threadIdx.x == 0) {
-    const long long u = blockIdx.x;
-    const int i = __ldg(unit_item + u);
-    ctx.it = items[i];
-    ctx.s = *ctx.it.sphere;
-    ctx.local = u - __ldg(starts + i);
+// Stage item i's context when it differs from the one staged (uniform across
+// the CTA); returns the unit's index within its item.
+__device__ __forceinline__ long long batch_unit(BatchCtx& ctx, int& staged, const qgb_batch_item* __restrict__ items,
+                                                const int* __restrict__ unit_item,
+                                                const long long* __restrict__ starts, long long u) {
+  const int i = __ldg(unit_item + u);
+  if (i != staged) {
+    if (threadIdx.x == 0) {
+      ctx.it = items[i];
+      ctx.s = *ctx.it.sphere;
+    }
+    staged = i;
+    __syncthreads();
   }
-  __syncthreads();
+  return u - __ldg(starts + i);
 }
+
+#define QGB_BATCH_UNITS_BEGIN                                                       \
+  __shared__ BatchCtx ctx;                                                          \
+  int staged = -1;                                                                  \
+  const long long u_begin = static_cast<long long>(blockIdx.x) * upc;               \
+  const long long u_end = u_begin + upc < n_units ? u_begin + upc : n_units;        \
+  for (long long u = u_begin; u < u_end; ++u) {                                     \
+    const long long local = batch_unit(ctx, staged, items, unit_item, starts, u);   \
+    const qgb_sphere& s = ctx.s;                                                    \
+    const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
+#define QGB_BATCH_UNITS_END                                                         \
+    __syncthreads(); /* shared memory and ctx are reused by the next unit */        \
+  }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_ifft_yz_batched(const qgb_batch_item* __restrict__ items,
                                                               const int* __restrict__ unit_item,
-                                                              const long long* __restrict__ starts) {
-  __shared__ BatchCtx ctx;
-  load_batch_ctx(ctx, items, unit_item, starts);
-  const qgb_sphere& s = ctx.s;
-  const int slab = static_cast<int>(ctx.local % s.max_slabs);
-  const long long rest = ctx.local / s.max_slabs;
-  const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
+                                                              const long long* __restrict__ starts,
+                                                              long long n_units, int upc) {
+  QGB_BATCH_UNITS_BEGIN
+  const int slab = static_cast<int>(local % s.max_slabs);
+  const long long rest = local / s.max_slabs;
   body_ifft_yz<T>(s, lp, static_cast<const cplx_t<T>*>(ctx.it.C), static_cast<cplx_t<T>*>(ctx.it.planes), slab,
                   static_cast<int>(rest % ctx.it.nb), static_cast<int>(rest / ctx.it.nb));
+  QGB_BATCH_UNITS_END
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_xpass_batched(const qgb_batch_item* __restrict__ items,
                                                             const int* __restrict__ unit_item,
-                                                            const long long* __restrict__ starts) {
-  __shared__ BatchCtx ctx;
-  load_batch_ctx(ctx, items, unit_item, starts);
-  const qgb_sphere& s = ctx.s;
-  const int r1 = static_cast<int>(ctx.local % s.N[1]);
-  const long long rest = ctx.local / s.N[1];
-  const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
+                                                            const long long* __restrict__ starts,
+                                                            long long n_units, int upc) {
+  QGB_BATCH_UNITS_BEGIN
+  const int r1 = static_cast<int>(local % s.N[1]);
+  const long long rest = local / s.N[1];
   const int b = static_cast<int>(rest % ctx.it.nb), k = static_cast<int>(rest / ctx.it.nb);
   if (sizeof(T) == 4 && s.N[2] % 4 == 0)
     body_xpass_async<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k, 0, s.N[2]);
   else
     body_xpass<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k);
+  QGB_BATCH_UNITS_END
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_fft_yz_gather_batched(const qgb_batch_item* __restrict__ items,
                                                                     const int* __restrict__ unit_item,
-                                                                    const long long* __restrict__ starts) {
-  __shared__ BatchCtx ctx;
-  load_batch_ctx(ctx, items, unit_item, starts);
-  const qgb_sphere& s = ctx.s;
-  const int slab = static_cast<int>(ctx.local % s.max_slabs);
-  const long long rest = ctx.local / s.max_slabs;
-  const LocalParams lp{ctx.it.nb, 0, ctx.it.nb, ctx.it.flags};
+                                                                    const long long* __restrict__ starts,
+                                                                    long long n_units, int upc) {
+  QGB_BATCH_UNITS_BEGIN
+  const int slab = static_cast<int>(local % s.max_slabs);
+  const long long rest = local / s.max_slabs;
   body_fft_yz_gather<T>(s, lp, static_cast<const cplx_t<T>*>(ctx.it.C), static_cast<cplx_t<T>*>(ctx.it.out),
                         static_cast<const cplx_t<T>*>(ctx.it.planes), slab, static_cast<int>(rest % ctx.it.nb),
                         static_cast<int>(rest / ctx.it.nb));
+  QGB_BATCH_UNITS_END
 }
 
 template <typename T>
@@ -715,12 +731,16 @@ static int launch_batched(const qgb_batch_item* items, const int* slab_item, con
     configured_x = smem_x;
   }
   lock.unlock();
-  k_ifft_yz_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem_yz, st>>>(items, slab_item, slab_starts);
+  // Units per CTA: up to 8 while the grid keeps at least 32 CTAs per SM.
+  auto upc_for = [](long long n) { return static_cast<int>(std::max(1LL, std::min(8LL, n / (152LL * 32)))); };
+  auto ctas = [](long long n, int upc) { return static_cast<unsigned>((n + upc - 1) / upc); };
+  const int us = upc_for(n_slab), ur = upc_for(n_row);
+  k_ifft_yz_batched<T><<<ctas(n_slab, us), kThreads, smem_yz, st>>>(items, slab_item, slab_starts, n_slab, us);
   QGB_LAUNCH_CHECK("k_ifft_yz_batched");
-  k_xpass_batched<T><<<static_cast<unsigned>(n_row), kThreads, smem_x, st>>>(items, row_item, row_starts);
+  k_xpass_batched<T><<<ctas(n_row, ur), kThreads, smem_x, st>>>(items, row_item, row_starts, n_row, ur);
   QGB_LAUNCH_CHECK("k_xpass_batched");
-  k_fft_yz_gather_batched<T><<<static_cast<unsigned>(n_slab), kThreads, smem_yz, st>>>(items, slab_item,
-                                                                                        slab_starts);
+  k_fft_yz_gather_batched<T><<<ctas(n_slab, us), kThreads, smem_yz, st>>>(items, slab_item, slab_starts, n_slab,
+                                                                          us);
   QGB_LAUNCH_CHECK("k_fft_yz_gather_batched");
   return QGB_OK;
 }

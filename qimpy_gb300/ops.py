@@ -147,20 +147,26 @@ def beta_split(beta: torch.Tensor) -> torch.Tensor:
 
 
 def apply_nonlocal_tc(split: torch.Tensor, D_blocks: torch.Tensor, C: torch.Tensor, HC: torch.Tensor,
-                      projT: torch.Tensor | None = None, ws: torch.Tensor | None = None):
-    """HC += beta D <beta|C> on the tensor cores (complex64); returns projT (nk, nb, P)."""
+                      projT: torch.Tensor | None = None, ws: torch.Tensor | None = None, phases: int = 3):
+    """HC += beta D <beta|C> on the tensor cores (complex64); returns projT (nk, nb, P).
+
+    phases = 1 runs only the part that reads C (projT and the back-projection
+    operand, kept in `ws`), phases = 2 the accumulation into HC from that `ws`."""
     nk, nb, n_tot = C.shape
     n_atoms, pa, _ = D_blocks.shape
     P = n_atoms * pa
     if C.dtype != torch.complex64 or HC.dtype != torch.complex64 or D_blocks.dtype != torch.complex64:
         raise TypeError("tensor-core nonlocal needs complex64 C, HC and D")
     projT = torch.empty((nk, nb, P), dtype=torch.complex64, device=C.device) if projT is None else projT
+    if phases != 3 and ws is None:
+        raise ValueError("a split nonlocal apply needs a caller-owned workspace")
     if ws is None:
         ws = workspace(int(_lib.lib().qgb_nonlocal_tc_workspace_bytes(nk, P, nb, n_tot)), C.device)
     err = device_error_word(C.device)
-    _lib.check(_lib.lib().qgb_apply_nonlocal_tc(split.data_ptr(), D_blocks.data_ptr(), n_atoms, pa, C.data_ptr(),
-                                                HC.data_ptr(), projT.data_ptr(), nk, nb, n_tot, ws.data_ptr(),
-                                                ws.numel(), err.data_ptr(), _stream()), "apply_nonlocal_tc")
+    _lib.check(_lib.lib().qgb_apply_nonlocal_tc_phase(split.data_ptr(), D_blocks.data_ptr(), n_atoms, pa,
+                                                      C.data_ptr(), HC.data_ptr(), projT.data_ptr(), nk, nb, n_tot,
+                                                      ws.data_ptr(), ws.numel(), err.data_ptr(), phases, _stream()),
+               "apply_nonlocal_tc")
     return projT
 
 

@@ -31,11 +31,14 @@ def _small_specs():
     return specs
 
 
-def test_batched_equals_individual_and_graph_replay():
+@pytest.mark.parametrize("chunk", [64 << 20, 1, 0])  # default, one instance per chunk, one chunk per group
+def test_batched_equals_individual_and_graph_replay(chunk):
     specs = _small_specs()
     insts = [bt.Instance(s, DEV) for s in specs]
     assert len({i.tables.shape for i in insts}) > 1  # uneven grids
-    bh = bt.BatchedHamiltonian(insts, torch.device(DEV))
+    bh = bt.BatchedHamiltonian(insts, torch.device(DEV), plane_chunk_bytes=chunk)
+    if chunk == 1:
+        assert sum(len(g._chunks) for g in bh.groups) == len(insts)
     bh.apply()
     torch.cuda.synchronize()
     eager = [o.clone() for o in bh.outputs]
