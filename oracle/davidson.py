@@ -123,6 +123,7 @@ class DavidsonResult:
     converged: bool
     deig_max: float
     hpsi_bands: int  #: band-applications of H performed
+    HC: np.ndarray = None  #: H C carried through the rotations (as the reference keeps it)
 
 
 def davidson(
@@ -188,4 +189,4 @@ def davidson(
         if n_eigs_done >= n_bands:
             converged = True
             break
-    return DavidsonResult(eig, C, i_iter, converged, deig_max, hpsi_bands)
+    return DavidsonResult(eig, C, i_iter, converged, deig_max, hpsi_bands, HC)

@@ -178,17 +178,54 @@ def run_case(qimpy, name: str, cfg: dict, out_dir: str) -> None:
           + (f"; Davidson {out['davidson_iterations']} it, {out['davidson_seconds']:.1f} s" if dav else ""))
 
 
+#: workload -> CheFSI settings (second caller of the Hamiltonian)
+CHEFSI_CASES = {
+    "tiny_fcc": dict(n_iterations=100, eig_threshold=1e-11, filter_order=10, init_threshold=1e-1),
+    "tiny_ortho": dict(n_iterations=100, eig_threshold=1e-11, filter_order=10, init_threshold=1e-1),
+    "si2": dict(n_iterations=100, eig_threshold=1e-10, filter_order=8, init_threshold=1e-1),
+}
+
+
+def run_chefsi_case(qimpy, name: str, cfg: dict, out_dir: str) -> None:
+    """Reference CheFSI (qimpy/dft/electrons/_chefsi.py:72-176) from the same
+    orthonormalised start vectors as the Davidson case: its Davidson warm-up
+    to init_threshold, then Chebyshev-filtered subspace iterations."""
+    import torch
+    from qimpy.dft.electrons import CheFSI, Wavefunction
+
+    t0 = time.time()
+    prob = wl.get(name)
+    mine = wl.make_basis(prob.Gbasis, prob.k, prob.ke_cutoff, prob.grid_shape)
+    system = build_system(qimpy, prob, None)
+    el = inject(qimpy, system, prob, wl.make_projectors(prob, mine))
+    C0 = wl.make_wavefunctions(prob, mine, prob.n_bands + prob.n_bands_extra)
+    el.C = Wavefunction(el.basis, coeff=torch.from_numpy(C0[None, :, :, None, :]).clone()).orthonormalize()
+    el.deig_max = np.inf
+    solver = CheFSI(electrons=el, **cfg)
+    solver()
+    out = dict(eig=el.eig[0].numpy().copy(), iterations=np.int64(solver._i_iter),
+               **{k: np.float64(v) for k, v in cfg.items()})
+    path = os.path.join(out_dir, f"chefsi_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"chefsi {name}: wrote {path}; {solver._i_iter} iterations in {time.time() - t0:.1f} s")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
     ap.add_argument("--only", nargs="*", default=None)
     ap.add_argument("--out", default=HERE)
+    ap.add_argument("--chefsi", action="store_true", help="only the CheFSI goldens")
     args = ap.parse_args()
     qimpy = import_reference(args.ref)
     for name, cfg in CASES.items():
-        if args.only and name not in args.only:
+        if args.chefsi or (args.only and name not in args.only):
             continue
         run_case(qimpy, name, cfg, args.out)
+    for name, cfg in CHEFSI_CASES.items():
+        if args.only and name not in args.only:
+            continue
+        run_chefsi_case(qimpy, name, cfg, args.out)
 
 
 if __name__ == "__main__":

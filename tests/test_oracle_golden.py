@@ -78,3 +78,19 @@ def test_oracle_davidson_rejects_oversized_subspace():
     p, b, beta, C = _problem("tiny_fcc", 60)
     with pytest.raises(ValueError):
         od.davidson(lambda X: X, C, b.ke, b.n, 50)
+
+
+@pytest.mark.parametrize("name", ["tiny_fcc", "tiny_ortho", "si2"])
+def test_oracle_chefsi_matches_reference_chefsi(name):
+    from oracle import chefsi as oc
+
+    g = np.load(os.path.join(GOLDEN, f"chefsi_{name}.npz"))
+    pw = wl.get(name)
+    p, b, beta, C = _problem(name, pw.n_bands + pw.n_bands_extra)
+    H = lambda X: oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, p.D_all(), X)  # noqa: E731
+    r = oc.chefsi(H, od.orthonormalize(C), b.ke, b.n, p.n_bands, p.ke_cutoff, float(p.V_r.max()),
+                  int(g["n_iterations"]), float(g["eig_threshold"]), int(g["filter_order"]),
+                  float(g["init_threshold"]))
+    assert r.converged
+    assert np.abs(r.eig[:, : p.n_bands] - g["eig"][:, : p.n_bands]).max() < 1e-10
+    assert r.iterations == int(g["iterations"])
