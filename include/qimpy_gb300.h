@@ -166,6 +166,18 @@ int qgb_apply_potential_static(const qgb_sphere* s, int dtype, const void* C, vo
 size_t qgb_static_scratch_bytes(void);
 
 /*
+ * Electron density of a band block: rho[N0][N1][N2] (FP64, natural real-space
+ * order) = sum_{k,b} prefac[k][b] |psi_kb(r)|^2 with psi = the unnormalised
+ * inverse FFT of the sphere-scattered C (complex128 or complex64 by dtype);
+ * prefac [nk][nb] FP64 = f * w_sk / Omega.  rho is zeroed first unless flags
+ * has QGB_ACCUMULATE.  Workspace as qgb_apply_potential (band chunks).
+ * Replaces Basis.collect_density (qimpy/dft/electrons/_basis_ops.py:207-296,
+ * one spin, no spinors) with accum_norm_ (qimpy/math/_linalg.py:31-58).
+ */
+int qgb_collect_density(const qgb_sphere* s, int dtype, const void* C, int nb, const double* prefac, double* rho,
+                        unsigned flags, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Shared memory per CTA the local-potential kernels need for a sphere (host):
  * the largest over the three kernels (the x-phase kernel's), and that of the
  * two y/z-phase kernels alone.

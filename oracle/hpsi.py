@@ -75,3 +75,20 @@ def hamiltonian(ke, V_r, fft_index, n, beta, D_all, C) -> np.ndarray:
     if beta is not None and beta.shape[1]:
         HC += apply_nonlocal(beta, D_all, project(beta, C))
     return HC
+
+
+def collect_density(fft_index: np.ndarray, shape, C: np.ndarray, prefac: np.ndarray) -> np.ndarray:
+    """rho(r) = sum_kb prefac[k, b] |psi_kb(r)|^2 with psi = ifft(scatter(C)) (no
+    scaling), prefac = f * w_sk / Omega; real-space grid in natural order.
+
+    Follows qimpy/dft/electrons/_basis_ops.py:207-296 (single spin, no spinor):
+    expand_ifft of every band (152-163) and accum_norm_ (qimpy/math/_linalg.py:31-58)."""
+    nk, nb, n_tot = C.shape
+    N = int(np.prod(shape))
+    rho = np.zeros(tuple(shape))
+    for k in range(nk):
+        grid = np.zeros((nb, N), dtype=np.complex128)
+        grid[:, fft_index[k]] = C[k]
+        psi_r = sfft.ifftn(grid.reshape((nb,) + tuple(shape)), axes=(1, 2, 3), norm="forward", workers=_WORKERS)
+        rho += np.einsum("b,bxyz->xyz", prefac[k], np.abs(psi_r) ** 2)
+    return rho

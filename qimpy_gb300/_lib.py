@@ -68,6 +68,8 @@ _SIGS = {
     "qgb_apply_potential_static": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
                                               ct.c_uint, ct.c_void_p]),
     "qgb_static_scratch_bytes": (ct.c_size_t, []),
+    "qgb_collect_density": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p,
+                                       ct.c_void_p, ct.c_uint, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
     "qgb_sphere_smem_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int]),
     "qgb_sphere_smem_bytes_yz": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.c_int]),
     "qgb_apply_potential_batched": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,

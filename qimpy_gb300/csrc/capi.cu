@@ -29,7 +29,7 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 
-int validate_sphere(const qgb_sphere* s, int dtype);
+int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true);
 size_t plane_bytes_per_band(const qgb_sphere& s, int dtype);
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
                     void* ws, size_t ws_bytes, cudaStream_t st);
@@ -42,6 +42,8 @@ int apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int 
 int debug_violation(unsigned long long* out4);
 #endif
 size_t sphere_smem_bytes(const qgb_sphere& s, int dtype);
+int collect_density(const qgb_sphere* s, int dtype, const void* C, int nb, const double* prefac, double* rho,
+                    unsigned flags, void* ws, size_t ws_bytes, cudaStream_t st);
 size_t plane_smem_bytes(const qgb_sphere& s, int dtype);
 int apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,
                             const long long* slab_starts, const int* row_item, const long long* row_starts,
@@ -168,6 +170,12 @@ int qgb_debug_violation(unsigned long long* out4) { return qgb::debug_violation(
 #endif
 
 size_t qgb_sphere_smem_bytes(const qgb_sphere* s, int dtype) { return s ? sphere_smem_bytes(*s, dtype) : 0; }
+
+int qgb_collect_density(const qgb_sphere* s, int dtype, const void* C, int nb, const double* prefac, double* rho,
+                        unsigned flags, void* workspace, size_t workspace_bytes, void* stream) {
+  return collect_density(s, dtype, C, nb, prefac, rho, flags, workspace, workspace_bytes,
+                         static_cast<cudaStream_t>(stream));
+}
 size_t qgb_sphere_smem_bytes_yz(const qgb_sphere* s, int dtype) { return s ? plane_smem_bytes(*s, dtype) : 0; }
 
 int qgb_apply_potential_batched(const qgb_batch_item* items, int n_items, const int* slab_item,

@@ -595,7 +595,7 @@ static size_t xpass_async_smem_bytes(const qgb_sphere& s) {
   return cplx * 8 + static_cast<size_t>(s.N[0]) * s.N[2] * 4;
 }
 
-int validate_sphere(const qgb_sphere* s, int dtype) {
+int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true) {
   if (s == nullptr) return fail(QGB_ERR_INVALID, "sphere descriptor is NULL");
   if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
   if (s->nk < 1 || s->n_tot < 1 || s->max_slabs < 1)
@@ -610,8 +610,9 @@ int validate_sphere(const qgb_sphere* s, int dtype) {
   }
   if (s->max_slabs > s->N[0]) return fail(QGB_ERR_INVALID, "max_slabs %d > N0", s->max_slabs);
   if (!s->n || !s->n_slabs || !s->slab_start || !s->slab_i0 || !s->yz || !s->row_start ||
-      !s->rows || !s->twiddle || !s->ke || !s->V)
+      !s->rows || !s->twiddle || !s->ke)
     return fail(QGB_ERR_INVALID, "sphere descriptor has a NULL table");
+  if (need_potential && !s->V) return fail(QGB_ERR_INVALID, "sphere descriptor has no potential V");
   if (plane_smem_bytes(*s, dtype) > 227 * 1024 || (xpass_async_ok(*s, dtype) && xpass_async_smem_bytes(*s) > 227 * 1024))
     return fail(QGB_ERR_UNSUPPORTED, "grid %dx%dx%d needs %zu B of shared memory per plane (max 227 KB)",
                 s->N[0], s->N[1], s->N[2], plane_smem_bytes(*s, dtype));
@@ -774,6 +775,160 @@ int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, c
   else
     k_apply_ke<float><<<blocks, 256, 0, st>>>(*s, nb, static_cast<const float2*>(C), static_cast<float2*>(out));
   QGB_LAUNCH_CHECK("k_apply_ke");
+  return QGB_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Density: rho(r) = sum_kb prefac[k][b] |psi_kb(r)|^2, psi = IFFT(scatter(C))
+// (replaces Basis.collect_density, qimpy/dft/electrons/_basis_ops.py:207-296,
+// single spin without spinors, with accum_norm_ of qimpy/math/_linalg.py:31-58).
+// k_ifft_yz leaves each band's slab planes (y, z inverse-transformed); then
+// k_density_x, one CTA per (k, y-row, z-range, group of bands): for each band
+// of its group it stages the slab rows of its y-row, runs the inverse x-FFT and
+// adds prefac |psi|^2 into per-thread register accumulators, and at the end
+// adds them into rho (natural real-space order) with one atomicAdd per grid
+// point.  rho is FP64 for both precisions.
+// ---------------------------------------------------------------------------
+
+template <typename T> struct DensityRegs { static constexpr int value = sizeof(T) == 4 ? 64 : 32; };
+
+__device__ __forceinline__ int digit_perm(int p, int L1, int L2) { return p / L1 + L2 * (p - (p / L1) * L1); }
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_density_x(const qgb_sphere s, LocalParams lp,
+                                                        const cplx_t<T>* __restrict__ planes,
+                                                        const double* __restrict__ prefac, double* __restrict__ rho,
+                                                        int zs, int bpc) {
+  using C2 = cplx_t<T>;
+  constexpr int R = DensityRegs<T>::value;
+  const int N0 = s.N[0], N1 = s.N[1], N2 = s.N[2];
+  const int r1 = blockIdx.x / zs, zp = blockIdx.x - r1 * zs;
+  const int nz_max = (N2 + zs - 1) / zs, z0 = zp * nz_max;
+  const int nz = min(nz_max, N2 - z0);
+  const int k = blockIdx.z;
+  if (nz <= 0) return;
+  const int ld = nz + 1, lim = N0 * ld, Wx = lim;
+  C2* sm = smem_c<T>();
+  const C2* tw = static_cast<const C2*>(s.twiddle);
+  load_twiddles<T>(Wx, tw + s.tw_off[0], N0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int nslabs = s.n_slabs[k];
+  const int* i0 = s.slab_i0 + k * s.max_slabs;
+  const size_t plane = static_cast<size_t>(N1) * N2;
+  const int total = N0 * nz;  // <= R * kThreads (host-checked)
+  const int step_px = kThreads / nz, step_c = kThreads - step_px * nz;
+  T acc[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) acc[j] = T(0);
+  const int b_begin = blockIdx.y * bpc, b_end = min(lp.nb, b_begin + bpc);
+  for (int b = b_begin; b < b_end; ++b) {
+    for (int r = warp; r < N0; r += nwarps)
+      for (int c = lane; c < nz; c += 32) sm[r * ld + c] = mk<T>(T(0), T(0));
+    __syncthreads();
+    if (!QGB_OK_IDX(plane_index(s, k, b, lp.nb, 0), (long long)s.nk * lp.nb * s.max_slabs, 20)) return;
+    const C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2 + z0;
+    for (int sl = warp; sl < nslabs; sl += nwarps) {
+      const int x = i0[sl];
+      for (int c = lane; c < nz; c += 32) sm[x * ld + c] = base[sl * plane + c];
+    }
+    __syncthreads();
+    fft_inverse<T>(0, nullptr, nz, 1, ld, s.L1[0], s.L2[0], Wx, lim);  // ends with __syncthreads
+    const T w = static_cast<T>(prefac[static_cast<size_t>(k) * lp.nb_total + lp.b0 + b]);
+    int px = threadIdx.x / nz, c = threadIdx.x - (threadIdx.x / nz) * nz;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      if (j * kThreads + static_cast<int>(threadIdx.x) < total) {
+        const C2 v = sm[px * ld + c];
+        acc[j] += w * (v.x * v.x + v.y * v.y);
+      }
+      px += step_px;
+      c += step_c;
+      if (c >= nz) {
+        c -= nz;
+        ++px;
+      }
+    }
+    __syncthreads();  // the tile is refilled for the next band
+  }
+  // Natural real-space order: every axis of the stored data is digit-permuted.
+  const int y = digit_perm(r1, s.L1[1], s.L2[1]);
+  int px = threadIdx.x / nz, c = threadIdx.x - (threadIdx.x / nz) * nz;
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    if (j * kThreads + static_cast<int>(threadIdx.x) < total) {
+      const int x = digit_perm(px, s.L1[0], s.L2[0]);
+      const int z = digit_perm(z0 + c, s.L1[2], s.L2[2]);
+      atomicAdd(rho + (static_cast<size_t>(x) * N1 + y) * N2 + z, static_cast<double>(acc[j]));
+    }
+    px += step_px;
+    c += step_c;
+    if (c >= nz) {
+      c -= nz;
+      ++px;
+    }
+  }
+}
+
+static int density_zsplit(const qgb_sphere& s, int dtype) {
+  const long long cap = static_cast<long long>(dtype == QGB_F64 ? DensityRegs<double>::value
+                                                                : DensityRegs<float>::value) * kThreads;
+  int zs = 1;
+  while (static_cast<long long>(s.N[0]) * ((s.N[2] + zs - 1) / zs) > cap) ++zs;
+  return zs;
+}
+
+template <typename T>
+static int launch_density_chunk(const qgb_sphere& s, const LocalParams& lp, const void* C, void* planes,
+                                const double* prefac, double* rho, size_t smem_yz, cudaStream_t st) {
+  using C2 = cplx_t<T>;
+  const dim3 g1(s.max_slabs, lp.nb, s.nk);
+  k_ifft_yz<T><<<g1, kThreads, smem_yz, st>>>(s, lp, static_cast<const C2*>(C), static_cast<C2*>(planes));
+  QGB_LAUNCH_CHECK("k_ifft_yz");
+  const int zs = density_zsplit(s, sizeof(T) == 8 ? QGB_F64 : QGB_F32);
+  const int nz = (s.N[2] + zs - 1) / zs;
+  const size_t smem = (static_cast<size_t>(s.N[0]) * (nz + 1) + s.N[0]) * sizeof(C2);
+  {
+    static size_t configured = 0;
+    std::lock_guard<std::mutex> lock(g_attr_mu);
+    if (smem > configured) {
+      QGB_CUDA_CHECK(cudaFuncSetAttribute(k_density_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      configured = smem;
+    }
+  }
+  // Groups of bands per CTA: enough CTAs to cover the SMs a few times over.
+  const long long base = static_cast<long long>(s.N[1]) * zs * s.nk;
+  const int groups = static_cast<int>(std::min<long long>(lp.nb, std::max<long long>(1, (4LL * 152 + base - 1) / base)));
+  const int bpc = (lp.nb + groups - 1) / groups;
+  const dim3 g2(s.N[1] * zs, (lp.nb + bpc - 1) / bpc, s.nk);
+  k_density_x<T><<<g2, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(planes), prefac, rho, zs, bpc);
+  QGB_LAUNCH_CHECK("k_density_x");
+  return QGB_OK;
+}
+
+int collect_density(const qgb_sphere* s, int dtype, const void* C, int nb, const double* prefac, double* rho,
+                    unsigned flags, void* ws, size_t ws_bytes, cudaStream_t st) {
+  int rc = validate_sphere(s, dtype, false);  // the density needs no potential
+  if (rc) return rc;
+  if (nb < 0) return fail(QGB_ERR_INVALID, "nb = %d < 0", nb);
+  if (!rho) return fail(QGB_ERR_INVALID, "NULL density pointer");
+  const size_t N = static_cast<size_t>(s->N[0]) * s->N[1] * s->N[2];
+  if (!(flags & QGB_ACCUMULATE)) QGB_CUDA_CHECK(cudaMemsetAsync(rho, 0, N * sizeof(double), st));
+  if (nb == 0) return QGB_OK;
+  if (!C || !prefac) return fail(QGB_ERR_INVALID, "NULL wavefunction or prefactor pointer");
+  const size_t per_band = plane_bytes_per_band(*s, dtype);
+  if (!ws || ws_bytes < per_band)
+    return fail(QGB_ERR_WORKSPACE, "workspace %zu B < %zu B needed for one band", ws_bytes, per_band);
+  const int chunk = static_cast<int>(std::min<size_t>(nb, std::min<size_t>(ws_bytes / per_band, 65535)));
+  const size_t smem = plane_smem_bytes(*s, dtype);
+  rc = (dtype == QGB_F64) ? set_smem_limits<double>(smem) : set_smem_limits<float>(smem);
+  if (rc) return rc;
+  for (int b0 = 0; b0 < nb; b0 += chunk) {
+    LocalParams lp{nb, b0, std::min(chunk, nb - b0), 0u};
+    rc = (dtype == QGB_F64) ? launch_density_chunk<double>(*s, lp, C, ws, prefac, rho, smem, st)
+                            : launch_density_chunk<float>(*s, lp, C, ws, prefac, rho, smem, st);
+    if (rc) return rc;
+  }
   return QGB_OK;
 }
 

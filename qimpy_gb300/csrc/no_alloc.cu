@@ -14,7 +14,7 @@
 
 namespace qgb {
 
-int validate_sphere(const qgb_sphere* s, int dtype);
+int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true);
 size_t plane_bytes_per_band(const qgb_sphere& s, int dtype);
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
                     void* ws, size_t ws_bytes, cudaStream_t st);

@@ -92,6 +92,18 @@ class Basis:
             self.set_potential(V)
         return Wavefunction(self, coeff=ops.apply_potential(self.sphere, C.coeff))
 
+    def collect_density(self, C: "Wavefunction", f: torch.Tensor, need_Mvec: bool = False) -> torch.Tensor:
+        """Electron density (qimpy/dft/electrons/_basis_ops.py:207-296) of the bands
+        of C with occupations f (nk, nb): rho(r) = sum_kb f w_sk / Omega |psi(r)|^2,
+        w_sk = 2 w_k (one spin, no spinors), as an FP64 (1, N0, N1, N2) tensor (the
+        reference's FieldR data with its one density component)."""
+        if need_Mvec:
+            raise NotImplementedError("magnetization densities need spinorial wavefunctions")
+        f = f.reshape(C.coeff.shape[0], C.n_bands()).to(torch.float64)
+        w_sk = 2.0 * torch.from_numpy(self.wk).to(f.device)
+        prefac = f * (w_sk[:, None] / self.volume)
+        return ops.collect_density(self.sphere, C.coeff, prefac)[None]
+
 
 class Ions:
     """Projectors and D matrix of the nonlocal pseudopotential."""

@@ -69,6 +69,27 @@ def apply_potential(sphere: DeviceSphere, C: torch.Tensor, out: torch.Tensor | N
     return out
 
 
+def collect_density(sphere: DeviceSphere, C: torch.Tensor, prefac: torch.Tensor, rho: torch.Tensor | None = None,
+                    accumulate: bool = False, ws: torch.Tensor | None = None) -> torch.Tensor:
+    """rho(r) (FP64, natural grid order, shape N0 x N1 x N2) = sum_kb prefac[k, b]
+    |psi_kb(r)|^2 of the bands in C; prefac (nk, nb) = f * w_sk / Omega."""
+    nb = _check_wf(sphere, C)
+    pf = prefac.to(device=C.device, dtype=torch.float64).contiguous()
+    if tuple(pf.shape) != (C.shape[0], nb):
+        raise ValueError(f"prefac shape {tuple(pf.shape)} != (nk, nb) = {(C.shape[0], nb)}")
+    if rho is None:
+        rho = torch.empty(sphere.shape, dtype=torch.float64, device=C.device)
+    elif rho.dtype != torch.float64 or tuple(rho.shape) != tuple(sphere.shape) or not rho.is_contiguous():
+        raise ValueError("rho must be a contiguous float64 tensor of the grid shape")
+    if ws is None:
+        ws = workspace(sphere.workspace_bytes(nb), C.device)
+    flags = _lib.QGB_ACCUMULATE if accumulate else 0
+    _lib.check(_lib.lib().qgb_collect_density(ct.byref(sphere.struct), sphere.qdtype, C.data_ptr(), nb,
+                                              pf.data_ptr(), rho.data_ptr(), flags, ws.data_ptr(), ws.numel(),
+                                              _stream()), "collect_density")
+    return rho
+
+
 def project(beta: torch.Tensor, C: torch.Tensor, projT: torch.Tensor | None = None) -> torch.Tensor:
     """projT[k, b, p] = <beta_p|C_b> (band-major projections)."""
     nk, P, n_tot = beta.shape

@@ -50,6 +50,15 @@ def splitmix_uniform_grid(seed: int, streams, counters) -> np.ndarray:
     return u + 0.5 / 9007199254740992.0  # strictly inside (0, 1)
 
 
+def make_fillings(prob: "Problem", nb: int, seed_stream: int = 11) -> np.ndarray:
+    """Seeded occupations f[k, b] in [0, 1] (one splitmix stream per workload):
+    a smeared step from 1 to 0 across the band window, perturbed by up to 5%."""
+    u = splitmix_uniform(prob.seed, seed_stream, prob.nk * nb).reshape(prob.nk, nb)
+    b = np.arange(nb)[None, :]
+    step = 1.0 / (1.0 + np.exp((b - 0.6 * nb) / max(1.0, 0.1 * nb)))
+    return np.clip(step * (0.95 + 0.1 * u), 0.0, 1.0)
+
+
 def splitmix_uniform(seed: int, stream: int, count: int) -> np.ndarray:
     """`count` uniforms in (0, 1) from one counter-based splitmix64 stream."""
     return splitmix_uniform_grid(seed, stream, np.arange(count, dtype=np.uint64))

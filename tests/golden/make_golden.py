@@ -210,22 +210,62 @@ def run_chefsi_case(qimpy, name: str, cfg: dict, out_dir: str) -> None:
     print(f"chefsi {name}: wrote {path}; {solver._i_iter} iterations in {time.time() - t0:.1f} s")
 
 
+#: workloads whose reference density is stored in full (others: checksums and samples)
+DENSITY_CASES = {"tiny_fcc": True, "tiny_ortho": True, "si2": False}
+
+
+def run_density_case(qimpy, name: str, full: bool, out_dir: str) -> None:
+    """Reference Basis.collect_density (qimpy/dft/electrons/_basis_ops.py:207-296)
+    of the seeded start vectors with seeded fillings: rho(r) = sum_kb f w_sk / Omega
+    |psi_kb(r)|^2 on the real-space grid (natural order)."""
+    import torch
+    from qimpy.dft.electrons import Wavefunction
+
+    prob = wl.get(name)
+    mine = wl.make_basis(prob.Gbasis, prob.k, prob.ke_cutoff, prob.grid_shape)
+    system = build_system(qimpy, prob, None)
+    el = inject(qimpy, system, prob, wl.make_projectors(prob, mine))
+    nb = prob.n_bands + prob.n_bands_extra
+    C0 = wl.make_wavefunctions(prob, mine, nb)
+    f = wl.make_fillings(prob, nb)
+    C = Wavefunction(el.basis, coeff=torch.from_numpy(C0[None, :, :, None, :]).clone())
+    rho = el.basis.collect_density(C, torch.from_numpy(f)[None].clone(), False).data[0].numpy()
+    out = dict(f=f, w_sk=el.basis.w_sk.numpy().reshape(-1).copy(), volume=np.float64(system.lattice.volume),
+               total=np.float64(rho.sum()), abs_total=np.float64(np.abs(rho).sum()),
+               plane_sums=rho.sum(axis=(1, 2)))
+    if full:
+        out["rho"] = rho
+    else:
+        idx = np.array([[0, 0, 0], [1, 2, 3], [5, 7, 11], [17, 4, 30]]) % np.array(rho.shape)
+        out["sample_idx"] = idx
+        out["sample"] = rho[idx[:, 0], idx[:, 1], idx[:, 2]]
+    path = os.path.join(out_dir, f"density_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"density {name}: wrote {path}; total {rho.sum():.6f}")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
     ap.add_argument("--only", nargs="*", default=None)
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--chefsi", action="store_true", help="only the CheFSI goldens")
+    ap.add_argument("--density", action="store_true", help="only the density goldens")
     args = ap.parse_args()
     qimpy = import_reference(args.ref)
+    only_part = args.chefsi or args.density
     for name, cfg in CASES.items():
-        if args.chefsi or (args.only and name not in args.only):
+        if only_part or (args.only and name not in args.only):
             continue
         run_case(qimpy, name, cfg, args.out)
     for name, cfg in CHEFSI_CASES.items():
-        if args.only and name not in args.only:
+        if (only_part and not args.chefsi) or (args.only and name not in args.only):
             continue
         run_chefsi_case(qimpy, name, cfg, args.out)
+    for name, full in DENSITY_CASES.items():
+        if (only_part and not args.density) or (args.only and name not in args.only):
+            continue
+        run_density_case(qimpy, name, full, args.out)
 
 
 if __name__ == "__main__":

@@ -94,3 +94,21 @@ def test_oracle_chefsi_matches_reference_chefsi(name):
     assert r.converged
     assert np.abs(r.eig[:, : p.n_bands] - g["eig"][:, : p.n_bands]).max() < 1e-10
     assert r.iterations == int(g["iterations"])
+
+
+@pytest.mark.parametrize("name", ["tiny_fcc", "tiny_ortho", "si2"])
+def test_oracle_density_matches_reference(name):
+    g = np.load(os.path.join(GOLDEN, f"density_{name}.npz"))
+    pw = wl.get(name)
+    p, b, beta, C = _problem(name, pw.n_bands + pw.n_bands_extra)
+    assert np.allclose(g["w_sk"], 2.0 * p.wk) and abs(float(g["volume"]) - p.volume) < 1e-12 * p.volume
+    f = wl.make_fillings(p, C.shape[1])
+    assert np.array_equal(f, g["f"])
+    rho = oh.collect_density(b.fft_index, p.grid_shape, C, f * (2.0 * p.wk[:, None] / p.volume))
+    scale = np.abs(rho).max()
+    if "rho" in g:
+        assert np.abs(rho - g["rho"]).max() <= 1e-12 * scale
+    else:
+        i = g["sample_idx"]
+        assert np.abs(rho[i[:, 0], i[:, 1], i[:, 2]] - g["sample"]).max() <= 1e-12 * scale
+    assert np.abs(rho.sum(axis=(1, 2)) - g["plane_sums"]).max() <= 1e-12 * np.abs(g["plane_sums"]).max()
