@@ -250,7 +250,7 @@ def roofline_counts(p, b, tables, nb_tile: int, real_bytes: int):
 # kernel, so planes one kernel writes and the next reads count as DRAM traffic
 # although they stay in L2 in a timed run).  Command and per-kernel figures:
 # profiles/ncu_local_si64_mixed.md.
-NCU_DRAM_BYTES_PER_BLOCK = {"local": 296.4e6, "nonlocal": 196.7e6}
+NCU_DRAM_BYTES_PER_BLOCK = {"local": 295.0e6, "nonlocal": 195.9e6}
 
 
 def local_roofline(rc, band_apps, t_loc, hbm_peak, peaks) -> dict:
