@@ -231,6 +231,13 @@ def make_workload(name: str):
     return p, b, beta, C
 
 
+def workload_config(args, ws: int) -> dict:
+    """The `config` of the JSON line (the same for both arms)."""
+    names = {"si64": "64-atom Si, 96^3 grid, n=37073, Gamma, 160 bands in blocks of 32, P=256"}
+    return {"workload": f"{args.workload}: {names.get(args.workload, 'see qimpy_gb300.workloads')}",
+            "l2": "flushed (512 MB write) between timed steps", "parallelism": f"replicas x{ws}"}
+
+
 def roofline_counts(p, b, tables, nb_tile: int, real_bytes: int):
     """Algorithmic bytes and flops per band-application."""
     N = int(np.prod(p.grid_shape))
@@ -668,7 +675,7 @@ def main():
         cb = cpu_baseline(args)
         out = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-               "dtype": "f64", "data": "synthetic", "config": {"workload": args.workload},
+               "dtype": "f64", "data": "synthetic", "config": workload_config(args, args.gpus),
                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                                            "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
@@ -693,8 +700,7 @@ def main():
         "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (f32)", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: 64-atom Si, 96^3 grid, n=37073, Gamma, 160 bands in blocks of 32, P=256",
-                   "l2": "flushed (512 MB write) between timed steps", "parallelism": f"replicas x{ws}"},
+        "config": workload_config(args, ws),
         "fp64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"], "e2e": f64.get("e2e"),
                  "clocks": f64["clocks"]},
         "mixed_over_fp64": mixed["value"] / f64["value"],
