@@ -239,7 +239,10 @@ def workload_config(args, ws: int) -> dict:
 
 
 def roofline_counts(p, b, tables, nb_tile: int, real_bytes: int):
-    """Algorithmic bytes and flops per band-application."""
+    """Algorithmic bytes and flops per band-application: local 2*5 N log2 N + 2N + 2n
+    flops and 2 n s_c + (N s_r + 4 n) / B_tile bytes (psi in, H psi out, V and the
+    sphere index shared by the B_tile bands of a block); nonlocal 2*8 P n + 8 P p_atom
+    flops and 2 n s_c + 2 P n s_c / B_tile bytes (beta read for both GEMMs)."""
     N = int(np.prod(p.grid_shape))
     n = float(b.n.mean())
     P = p.n_projectors

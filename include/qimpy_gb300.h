@@ -40,7 +40,7 @@ enum qgb_status {
   QGB_ERR_WORKSPACE = 2,   /* workspace smaller than qgb_*_workspace_bytes() */
   QGB_ERR_CUDA = 3,        /* CUDA runtime or launch error */
   QGB_ERR_CUBLAS = 4,      /* cuBLAS error */
-  QGB_ERR_UNSUPPORTED = 5, /* valid request this build does not implement */
+  QGB_ERR_UNSUPPORTED = 5, /* valid request the library does not implement */
   QGB_ERR_CUSOLVER = 6     /* cuSOLVER error */
 };
 
