@@ -9,6 +9,7 @@ ascending linear grid index, so points sharing the first grid index i0 (a
 from __future__ import annotations
 
 import ctypes as ct
+import dataclasses
 import math
 from dataclasses import dataclass
 
@@ -176,7 +177,7 @@ class DeviceSphere:
             inv = [np.argsort(p) for p in self.perms]
             p0, p1, p2 = (torch.from_numpy(i).to(self._V.device) for i in inv)
             V_real = self._V[p0][:, p1][:, :, p2]
-        self.tables.fac = fac
+        self.tables = dataclasses.replace(self.tables, fac=fac)  # the caller's tables stay as they were
         tw = np.concatenate([twiddle_table(self.shape[a], *fac[a]) for a in range(3)])
         self._tw = torch.from_numpy(tw).to(self.cdtype).to(self.device)
         self.perms = [permutation(self.shape[a], *fac[a]) for a in range(3)]
