@@ -160,33 +160,38 @@ class Davidson:
             C_HC_new = _tile_expansion(C_HC, (Cnew ^ HCexp).wait())
             # FP32 vectors: directions the expanded basis barely spans are below
             # its rounding and are dropped (canonical orthogonalisation).
-            eig_new, V_new = eighg(C_HC_new, C_OC_new, drop_below=1e-4 if fp32 else 0.0)
+            eig_new, V_new, failed = eighg(C_HC_new, C_OC_new, drop_below=1e-4 if fp32 else 0.0, check=False)
             n_bands_next = min(n_bands_new, n_bands_max)
-            if fp32 and bool(torch.isinf(eig_new[:, n_bands_next - 1]).any()):
+            # Everything the host needs from this iteration in one transfer:
+            # _check_deig (_davidson.py:126-139), the factorisation status and,
+            # for FP32, whether fewer usable directions than bands remain.
+            d = torch.abs(el.eig - eig_new[..., :n_bands_cur])[:, :n_bands]
+            pend = (d > self.eig_threshold).any(dim=0)
+            first_pending = torch.where(pend.any(), pend.int().argmax(), torch.tensor(n_bands, device=pend.device))
+            host = torch.stack((d.max(), first_pending.to(torch.float64), failed.any().to(torch.float64),
+                                torch.isinf(eig_new[:, n_bands_next - 1]).any().to(torch.float64))).tolist()
+            if host[2]:
+                raise RuntimeError("subspace eigenproblem failed: overlap not positive-definite or eigh did not converge")
+            if fp32 and host[3]:
                 # Fewer usable directions than retained bands: no usable update
                 # at FP32 precision.  Keep the current state.
                 stalled = True
                 break
-            prev = (el.C, el.eig, HC, el.deig_max)
+            deig_max = host[0]
+            if fp32 and min_deig < 1e-3 and deig_max > 100.0 * min_deig:
+                # FP32 rounding has started to feed back: keep the current state and stop.
+                stalled = True
+                break
             V_new = V_new[..., :n_bands_next]
             Vcur, Vexp = V_new[:, :n_bands_cur], V_new[:, n_bands_cur:]
             el.C = Cnew @ V_new
             HC = HC @ Vcur
             HC += HCexp @ Vexp
-            deig = torch.abs(el.eig - eig_new[..., :n_bands_cur])
             el.eig = eig_new[..., :n_bands_next]
-            # _check_deig (_davidson.py:126-139), one host sync per iteration:
-            d = deig[:, :n_bands]
-            el.deig_max = float(d.max())
-            if fp32 and min_deig < 1e-3 and el.deig_max > 100.0 * min_deig:
-                # FP32 rounding has started to feed back: revert and stop.
-                el.C, el.eig, HC, el.deig_max = prev
-                stalled = True
-                break
+            el.deig_max = deig_max
             if el.deig_max < min_deig:
                 min_deig, i_best = el.deig_max, self._i_iter
-            pending = torch.where((d > self.eig_threshold).any(dim=0))[0]
-            n_eigs_done = int(pending[0]) if len(pending) else n_bands
+            n_eigs_done = int(host[1])
             converged = n_eigs_done >= n_bands
             if converged and self.residual_threshold is not None:
                 # HC is carried by rotations and drifts from H C over many

@@ -16,11 +16,13 @@ import torch
 from . import _lib
 
 
-def eigh(A: torch.Tensor):
+def eigh(A: torch.Tensor, check: bool = True):
     """Eigenvalues (ascending) and eigenvectors of Hermitian FP64 matrices
     A [..., n, n] on a CUDA device, one batched cuSOLVER call
     (qgb_subspace_eigh) for all leading indices.  Raises if any fails to
-    converge (as torch.linalg.eigh does)."""
+    converge (as torch.linalg.eigh does); with check=False it returns
+    (E, V, failed) instead, `failed` a device bool per matrix, without the host
+    synchronisation the check needs."""
     if A.device.type != "cuda" or A.dtype != torch.complex128:
         raise TypeError(f"eigh needs complex128 CUDA matrices, got {A.dtype} on {A.device}")
     n = A.shape[-1]
@@ -29,6 +31,8 @@ def eigh(A: torch.Tensor):
     nk = X.shape[0]
     W = torch.empty((nk, n), dtype=torch.float64, device=A.device)
     if nk == 0 or n == 0:
+        if not check:
+            return W.reshape(*lead, n), X.reshape(*lead, n, n), torch.zeros(lead, dtype=torch.bool, device=A.device)
         return W.reshape(*lead, n), X.reshape(*lead, n, n)
     info = torch.empty(nk, dtype=torch.int32, device=A.device)
     lib = _lib.lib()
@@ -39,11 +43,14 @@ def eigh(A: torch.Tensor):
     st = torch.cuda.current_stream(A.device).cuda_stream
     _lib.check(lib.qgb_subspace_eigh(X.data_ptr(), W.data_ptr(), info.data_ptr(), nk, n, ws.data_ptr(),
                                      ws_bytes, ct.c_void_p(st)), "subspace_eigh")
+    # X holds V^H row-major (the column-major solve saw conj(A)).
+    V = X.conj().transpose(-2, -1).reshape(*lead, n, n)
+    if not check:
+        return W.reshape(*lead, n), V, (info != 0).reshape(lead)
     bad = torch.nonzero(info).flatten().tolist()
     if bad:
         raise RuntimeError(f"subspace eigh: (Batch element {bad[0]}) did not converge (info {int(info[bad[0]])})")
-    # X holds V^H row-major (the column-major solve saw conj(A)).
-    return W.reshape(*lead, n), X.conj().transpose(-2, -1).reshape(*lead, n, n)
+    return W.reshape(*lead, n), V
 
 
 def dagger(x: torch.Tensor) -> torch.Tensor:
@@ -72,7 +79,7 @@ def _canonical_ortho(O: torch.Tensor, drop_below: float):
     return V * scale[..., None, :].to(V.dtype), keep
 
 
-def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0):
+def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0, check: bool = True):
     """Solve H V = O V E (qimpy/math/_linalg.py:143-183); H may be a Waitable.
 
     drop_below > 0 is for overlaps of FP32 vectors.  Their rounding (and the
@@ -82,29 +89,47 @@ def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0
     direction (min L_ii^2 < drop_below * max O_ii, or a failed factorisation),
     the basis is orthonormalised canonically instead, dropping directions with
     eigenvalue below that floor.  Dropped directions come last, with
-    eigenvalue +inf and eigenvector zero."""
+    eigenvalue +inf and eigenvector zero.
+
+    check=False returns (E, V, failed) with `failed` a device bool per k (a
+    failed Cholesky factorisation of O, or an eigensolve that did not
+    converge), so that the caller can fold the test into its own host
+    synchronisation; check=True raises as the reference does."""
     Hr = H.wait() if hasattr(H, "wait") else H
     keep = None
-    if drop_below > 0.0 and use_cholesky:
+    chol_failed = None
+    if use_cholesky:
         eye = torch.eye(O.shape[-1], device=O.device, dtype=O.dtype).expand(O.shape)
         L, info = torch.linalg.cholesky_ex(O)
-        pivot = L.diagonal(dim1=-2, dim2=-1).real.square().amin(dim=-1)
-        floor = drop_below * O.diagonal(dim1=-2, dim2=-1).real.amax(dim=-1)
-        if bool(((info != 0) | (pivot < floor)).any()):
-            U, keep = _canonical_ortho(O, drop_below)
+        if drop_below > 0.0:
+            pivot = L.diagonal(dim1=-2, dim2=-1).real.square().amin(dim=-1)
+            floor = drop_below * O.diagonal(dim1=-2, dim2=-1).real.amax(dim=-1)
+            if bool(((info != 0) | (pivot < floor)).any()):
+                U, keep = _canonical_ortho(O, drop_below)
+        elif check:
+            bad = torch.nonzero(info).flatten().tolist()
+            if bad:
+                raise RuntimeError(f"linalg.cholesky: (Batch element {bad[0]}): the overlap is not positive-definite")
         else:
+            chol_failed = info != 0
+        if keep is None:
             U = dagger(torch.linalg.solve_triangular(L, eye, upper=False))
     else:
         U = ortho_matrix(O, use_cholesky)
     Hs = dagger(U) @ (Hr @ U)
-    if keep is None:
+    if keep is not None:
+        # Dropped directions: zero rows/columns of Hs; give them a diagonal above
+        # the spectral norm of the rest so that they sort last, then mark them +inf.
+        big = 10.0 * (torch.linalg.matrix_norm(Hs).amax() + 1.0)
+        Hs = Hs + torch.diag_embed((~keep).to(torch.float64) * big).to(Hs.dtype)
+    if check:
         E, V = eigh(Hs)
-        return E, U @ V
-    # Dropped directions: zero rows/columns of Hs; give them a diagonal above the
-    # spectral norm of the rest so that they sort last, then mark them +inf.
-    big = 10.0 * (torch.linalg.matrix_norm(Hs).amax() + 1.0)
-    Hs = Hs + torch.diag_embed((~keep).to(torch.float64) * big).to(Hs.dtype)
-    E, V = eigh(Hs)
-    n_keep = keep.sum(dim=-1, keepdim=True)
-    E = torch.where(torch.arange(E.shape[-1], device=E.device) >= n_keep, torch.full_like(E, math.inf), E)
-    return E, U @ V
+        failed = None
+    else:
+        E, V, failed = eigh(Hs, check=False)
+        if chol_failed is not None:
+            failed = failed | chol_failed
+    if keep is not None:
+        n_keep = keep.sum(dim=-1, keepdim=True)
+        E = torch.where(torch.arange(E.shape[-1], device=E.device) >= n_keep, torch.full_like(E, math.inf), E)
+    return (E, U @ V) if check else (E, U @ V, failed)
