@@ -40,6 +40,38 @@ class DavidsonStats:
     stalled: bool = False
 
 
+def _xorshift_randn(x: torch.Tensor) -> torch.Tensor:
+    """Complex normal deviates from a signed 64-bit xorshift state, advanced in
+    place (qimpy/dft/electrons/_wavefunction_init.py:11-24: shifts of torch
+    int64 are arithmetic, overflow wraps; Box-Muller from two uniforms)."""
+    u = []
+    for _ in range(2):
+        x ^= x << 13
+        x ^= x >> 7
+        x ^= x << 17
+        u.append((0.5 ** 64) * x.to(torch.float64) + 0.5)
+    return torch.sqrt(-2.0 * torch.log(u[0])) * torch.exp((2j * np.pi) * u[1])
+
+
+def randomize_selected(C: Wavefunction, i_k: torch.Tensor, i_band: torch.Tensor, seed: int) -> None:
+    """Seeded random bands (k, band) of C in place, one spin and one spinor
+    (qimpy/dft/electrons/_wavefunction_init.py:127-188): the state of every
+    coefficient is (1 + seed) + g + n_max (band + n_bands k), one warm-up draw,
+    then a complex normal; padding zeroed, damped by 1 / (1 + (4/3 KE)^6)."""
+    basis = C.basis
+    n_bands, n_tot = C.coeff.shape[1], C.coeff.shape[2]
+    dev = C.coeff.device
+    i_k, i_band = i_k.to(dev, torch.int64), i_band.to(dev, torch.int64)
+    n_max = int(basis.n_max)
+    g = torch.arange(n_tot, dtype=torch.int64, device=dev)
+    x = (1 + seed) + g[None, :] + n_max * (i_band[:, None] + n_bands * i_k[:, None])
+    _xorshift_randn(x)  # warm-up: discard one output after seeding
+    vals = _xorshift_randn(x)
+    vals = vals * basis.mask[i_k].to(vals.real.dtype) / (1.0 + ((4.0 / 3) * basis.ke[i_k]) ** 6)
+    C.coeff[i_k, i_band] = vals.to(C.coeff.dtype)
+    C._projT = None
+
+
 def _tile_expansion(C_XC: torch.Tensor, Cnew_XCexp: torch.Tensor) -> torch.Tensor:
     """Expanded subspace matrix (qimpy/dft/electrons/_davidson.py:240-264)."""
     nk, n_new, n_exp = Cnew_XCexp.shape
@@ -78,19 +110,14 @@ class Davidson:
         return Wavefunction(Cerr.basis, coeff=Cerr.coeff / x.to(Cerr.coeff.real.dtype))
 
     def _regularize(self, C: Wavefunction, norm: torch.Tensor, i_iter: int) -> None:
-        """Re-randomise null bands (qimpy/dft/electrons/_davidson.py:101-115)."""
+        """Re-randomise null bands (qimpy/dft/electrons/_davidson.py:101-115) with
+        the reference's seeded generator (randomize_selected, seed = i_iter)."""
         low = norm < self._norm_cut
         if not bool(low.any()):
             return
         i_k, i_b = torch.where(low)
-        basis = C.basis
-        g = torch.Generator(device="cpu").manual_seed(1000 + i_iter)
-        for k, b in zip(i_k.tolist(), i_b.tolist()):
-            v = torch.randn((basis.n_tot,), generator=g, dtype=torch.complex128)
-            v = v / (1.0 + ((4.0 / 3) * basis.ke[k].cpu()) ** 6)
-            C.coeff[k, b] = v.to(C.coeff.device, C.coeff.dtype)
-        C.constrain()
-        norm[i_k, i_b] = 1.0
+        randomize_selected(C, i_k, i_b, i_iter)
+        norm[i_k, i_b] = 1.0  # just an estimate, as in the reference
 
     def __call__(self, n_iterations: Optional[int] = None) -> DavidsonStats:
         """Run to convergence with direct H.psi calls."""

@@ -78,3 +78,24 @@ def test_product_path_fails_loudly_without_library(tmp_path):
         "    print('loaded')\n" % (ROOT, str(tmp_path / "missing.so")))
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
     assert "raised" in out.stdout, out.stdout + out.stderr
+
+
+def test_randomize_selected_matches_oracle():
+    """The GPU Davidson's null-band re-randomisation reproduces the reference's
+    seeded xorshift generator (restated in the oracle), run here on CPU tensors."""
+    from oracle import davidson as od
+    from qimpy_gb300 import davidson as dv
+    from qimpy_gb300.electrons import Wavefunction
+
+    rng = np.random.default_rng(3)
+    nk, nb, n_tot = 2, 5, 40
+    n = np.array([37, 40])
+    ke = rng.uniform(0.0, 3.0, (nk, n_tot))
+    mask = np.arange(n_tot)[None, :] < n[:, None]
+    basis = types.SimpleNamespace(n_max=int(n.max()), ke=torch.from_numpy(ke), mask=torch.from_numpy(mask))
+    C = Wavefunction(basis, coeff=torch.zeros((nk, nb, n_tot), dtype=torch.complex128))
+    i_k, i_b = np.array([0, 1, 1]), np.array([3, 0, 4])
+    dv.randomize_selected(C, torch.from_numpy(i_k), torch.from_numpy(i_b), seed=7)
+    want = np.zeros((nk, nb, n_tot), dtype=np.complex128)
+    od.randomize_selected(want, i_k, i_b, 7, n, int(n.max()), nk, ke)
+    assert np.allclose(C.coeff.numpy(), want, rtol=1e-13, atol=0)
