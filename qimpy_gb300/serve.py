@@ -20,7 +20,7 @@ import math
 import time
 import traceback
 from concurrent.futures import ThreadPoolExecutor
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Optional
 
 import numpy as np
@@ -131,8 +131,6 @@ class EigenServer:
     def estimate_bytes(self, spec: InstanceSpec, n_bands: int) -> int:
         """HBM held by an active request: wavefunction-sized Davidson arrays, the
         slab planes of one block, projectors (and their bf16 operands), V, tables."""
-        from .batch import reference_grid  # noqa: F401  (grid already in spec)
-
         N = spec.grid
         nk = len(spec.k)
         n_est = (2.0 * spec.ke_cutoff) ** 1.5 * spec.side ** 3 / (6 * math.pi ** 2) * 1.1

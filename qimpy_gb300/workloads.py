@@ -24,7 +24,6 @@ wrapped to [-1/2, 1/2) (qimpy/lattice/_kpoints.py:130-138).
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import Optional
 
 import numpy as np
 

@@ -8,7 +8,6 @@ import sys
 import types
 
 import numpy as np
-import pytest
 import torch
 
 from qimpy_gb300 import batch as bt

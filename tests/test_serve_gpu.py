@@ -3,7 +3,6 @@ alone and in a mix with other requests that arrive while it is on the GPU;
 failures stay isolated to their request."""
 import numpy as np
 import pytest
-import torch
 
 from qimpy_gb300 import batch as bt
 from qimpy_gb300 import serve as sv
