@@ -645,8 +645,8 @@ def run_serving(args, local):
                 pos = wl.supercell_positions(wl._DIAMOND_BASIS, 2)
                 specs[i] = bt.InstanceSpec(i, 20.52, pos, 20.0, 160, np.zeros((1, 3)), 41 * 100003 + i, grid=96)
         reqs = sv.poisson_stream(specs, rate_hz=200.0, seed=41)
-        srv = sv.EigenServer(dev, precision=precision, eig_threshold=1e-6)
-        rep = srv.run(reqs, realtime=True, max_wall_s=args.serve_wall)
+        with sv.EigenServer(dev, precision=precision, eig_threshold=1e-6) as srv:
+            rep = srv.run(reqs, realtime=True, max_wall_s=args.serve_wall)
         res = [r.residual for r in reqs if r.status == "done"]
         rep["residual_max"] = float(np.max(res)) if res else None
         rep["sample"] = f"{count} requests of the 200 req/s stream ({sum(u < 0.05)} Si64-like)"

@@ -116,6 +116,17 @@ class EigenServer:
         self.tick_wall: list = []  #: host seconds per tick
         self._hpsi_events: list = []  #: (start, end) CUDA events around each batched H.psi
 
+    def close(self) -> None:
+        """Stop the worker pools (after finishing what they run)."""
+        self._pool.shutdown(wait=True)
+        self._finisher.shutdown(wait=True)
+
+    def __enter__(self) -> "EigenServer":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
     def _warm_up(self) -> None:
         """Load the extension and torch's lazily loaded linear-algebra backends
         once on this thread: their first use from several worker threads at
