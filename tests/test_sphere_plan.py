@@ -129,3 +129,22 @@ def test_factorisation_and_permutation(N):
 def test_factorisation_rejects_large_primes():
     with pytest.raises(ValueError):
         sp.factor_axis(17 * 3)
+
+
+def test_batched_units_per_cta_cover_every_unit_once():
+    """CPU replay of the batched launch geometry (launch_batched and the
+    QGB_BATCH_UNITS_BEGIN loop): with upc = clamp(n / (152 * 32), 1, 8) units per
+    CTA and ceil(n / upc) CTAs, every work unit u < n runs exactly once and no
+    CTA touches u >= n."""
+    import numpy as np
+
+    for n in [1, 7, 152 * 32 - 1, 152 * 32, 152 * 32 * 3 + 5, 1_300_001]:
+        upc = max(1, min(8, n // (152 * 32)))
+        ctas = (n + upc - 1) // upc
+        seen = np.zeros(n, dtype=np.int64)
+        for b in range(ctas):
+            u0 = b * upc
+            u1 = min(u0 + upc, n)
+            assert u0 < n
+            seen[u0:u1] += 1
+        assert np.all(seen == 1)
