@@ -148,3 +148,41 @@ def test_batched_units_per_cta_cover_every_unit_once():
             assert u0 < n
             seen[u0:u1] += 1
         assert np.all(seen == 1)
+
+
+def test_density_kernel_index_replay():
+    """CPU replay of k_density_x's indexing: the z-split keeps N0 * nz within
+    the per-thread register accumulators (64 FP32 / 32 FP64 per thread, 256
+    threads), and the incremental (px, c) walk of each thread visits exactly
+    e = t + 256 j -> (e // nz, e % nz), covering the tile once."""
+    import numpy as np
+
+    threads = 256
+    for dtype_regs in (64, 32):
+        for N0, N2 in [(18, 18), (15, 25), (36, 36), (96, 96), (100, 100), (144, 120), (160, 160)]:
+            zs = 1
+            while N0 * ((N2 + zs - 1) // zs) > dtype_regs * threads:
+                zs += 1
+            nz_max = (N2 + zs - 1) // zs
+            covered = np.zeros((N0, N2), dtype=np.int64)
+            for zp in range(zs):
+                z0 = zp * nz_max
+                nz = min(nz_max, N2 - z0)
+                if nz <= 0:
+                    continue
+                total = N0 * nz
+                assert total <= dtype_regs * threads
+                step_px, step_c = threads // nz, threads - (threads // nz) * nz
+                for t in range(threads):
+                    px, c = t // nz, t - (t // nz) * nz
+                    for j in range(dtype_regs):
+                        e = t + j * threads
+                        if e < total:
+                            assert (px, c) == (e // nz, e % nz)
+                            covered[px, z0 + c] += 1
+                        px += step_px
+                        c += step_c
+                        if c >= nz:
+                            c -= nz
+                            px += 1
+            assert np.all(covered == 1), (N0, N2, dtype_regs)
