@@ -92,3 +92,66 @@ def collect_density(fft_index: np.ndarray, shape, C: np.ndarray, prefac: np.ndar
         psi_r = sfft.ifftn(grid.reshape((nb,) + tuple(shape)), axes=(1, 2, 3), norm="forward", workers=_WORKERS)
         rho += np.einsum("b,bxyz->xyz", prefac[k], np.abs(psi_r) ** 2)
     return rho
+
+
+# ---------------------------------------------------------------------------
+# Real (Gamma-point) wavefunctions: half-mesh basis, r2c / c2r FFTs
+# (qimpy/dft/electrons/_basis_real.py:10-106, _basis_ops.py:119-163 with
+# shapeH, qimpy/grid/_fft.py real dispatch, _wavefunction_dot.py:55-88).
+# ---------------------------------------------------------------------------
+
+
+def real_gweight(iG: np.ndarray, n: int, n_tot: int) -> np.ndarray:
+    """Overlap weight of each basis entry: 1 on the Gz = 0 plane, 2 elsewhere
+    (the implicit -G partner), 0 on padding (_basis_real.py:62-66)."""
+    w = np.where(iG[:, 2] == 0, 1.0, 2.0)
+    w[n:] = 0.0
+    return w[:n_tot]
+
+
+def real_symmetrize(C: np.ndarray, iG: np.ndarray, shape) -> np.ndarray:
+    """Hermitian Gz = 0 plane, c(G) = (c(G) + conj(c(-G))) / 2, in place
+    (BasisReal.symmetrize, _basis_real.py:68-106); iG is the k = 0 basis."""
+    N0, N1 = shape[0], shape[1]
+    z0 = np.flatnonzero(iG[:, 2] == 0)
+    key = (iG[z0, 0] % N0) * N1 + (iG[z0, 1] % N1)
+    key_conj = ((-iG[z0, 0]) % N0) * N1 + ((-iG[z0, 1]) % N1)
+    where = {int(kk): i for i, kk in enumerate(key)}
+    partner = np.array([where[int(kk)] for kk in key_conj])
+    cz = C[..., z0]
+    C[..., z0] = 0.5 * (cz + np.conj(cz[..., partner]))
+    return C
+
+
+def apply_potential_real(V_r: np.ndarray, fft_index: np.ndarray, n: np.ndarray, iG: np.ndarray,
+                         C: np.ndarray) -> np.ndarray:
+    """gather(rfft(V * irfft(scatter(C)))) on the half grid, then constrain
+    (padding zeroed, Gz = 0 plane symmetrised); norms as apply_potential."""
+    nk, nb, n_tot = C.shape
+    shape = V_r.shape
+    half = (shape[0], shape[1], shape[2] // 2 + 1)
+    out = np.empty_like(C)
+    for k in range(nk):
+        grid = np.zeros((nb, int(np.prod(half))), dtype=np.complex128)
+        grid[:, fft_index[k]] = C[k]
+        psi_r = sfft.irfftn(grid.reshape((nb,) + half), s=shape, axes=(1, 2, 3), norm="forward", workers=_WORKERS)
+        VC = sfft.rfftn(psi_r * V_r[None], axes=(1, 2, 3), norm="forward", workers=_WORKERS).reshape(nb, -1)
+        out[k] = VC[:, fft_index[k]]
+    constrain(out, n)
+    return real_symmetrize(out, iG[0], shape)
+
+
+def project_real(beta: np.ndarray, C: np.ndarray, gweight: np.ndarray) -> np.ndarray:
+    """<beta|C> of real wavefunctions: Re sum_G w_G conj(beta) C, as proj[k, p, b]
+    (the real-basis branch of _wavefunction_dot.py:55-88)."""
+    r = np.matmul(beta.conj() * gweight[None, None, :], np.swapaxes(C, 1, 2))
+    return r.real.astype(np.complex128)
+
+
+def hamiltonian_real(ke, V_r, fft_index, n, iG, beta, D_all, C, gweight) -> np.ndarray:
+    """HC = KE C + V C + beta D <beta|C> for real (Gamma-point) wavefunctions."""
+    HC = apply_ke(ke, C)
+    HC += apply_potential_real(V_r, fft_index, n, iG, C)
+    if beta is not None and beta.shape[1]:
+        HC += apply_nonlocal(beta, D_all, project_real(beta, C, gweight))
+    return HC

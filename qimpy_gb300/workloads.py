@@ -211,9 +211,21 @@ def grid_iG(shape) -> np.ndarray:
     return mesh.reshape(-1, 3).astype(np.int64)
 
 
-def make_basis(Gbasis: np.ndarray, k: np.ndarray, ke_cutoff: float, shape) -> BasisLayout:
-    """Plane-wave basis per k (restates qimpy/dft/electrons/_basis.py:167-204)."""
-    iG_grid = grid_iG(shape)
+def grid_iH(shape) -> np.ndarray:
+    """Integer half (Hermitian-symmetric) reciprocal mesh (N0*N1*(N2//2+1), 3) of
+    real-wavefunction bases: the full mesh's first N2//2 + 1 z-frequencies
+    (qimpy/grid/_grid.py get_mesh("H") with _fft.py:72-76)."""
+    iG1 = [np.where(np.arange(s) <= s // 2, np.arange(s), np.arange(s) - s) for s in shape]
+    iG1[2] = iG1[2][: shape[2] // 2 + 1]
+    mesh = np.stack(np.meshgrid(*iG1, indexing="ij"), axis=-1)
+    return mesh.reshape(-1, 3).astype(np.int64)
+
+
+def make_basis(Gbasis: np.ndarray, k: np.ndarray, ke_cutoff: float, shape, real: bool = False) -> BasisLayout:
+    """Plane-wave basis per k (restates qimpy/dft/electrons/_basis.py:167-204);
+    real=True: the half-mesh basis of real (Gamma-point) wavefunctions, with
+    fft_index into the N0 x N1 x (N2//2+1) half grid (_basis.py:168)."""
+    iG_grid = grid_iH(shape) if real else grid_iG(shape)
     n_fft = iG_grid.shape[0]
     G = (iG_grid[None, :, :] + k[:, None, :]) @ Gbasis.T
     ke_grid = 0.5 * np.square(G).sum(axis=-1)
@@ -458,7 +470,23 @@ def tiny_ortho(seed: int = 12, shape=(15, 20, 25)) -> Problem:
     return _finish(prob, 1.5, 1.0, 0.2)
 
 
-WORKLOADS = {"si2": si2, "si64": si64, "cu32": cu32, "tiny_fcc": tiny_fcc, "tiny_ortho": tiny_ortho}
+def tiny_gamma(seed: int = 13, shape=(16, 20, 24)) -> Problem:
+    """Gamma-only orthorhombic cell for real wavefunctions (half-mesh basis,
+    qimpy/dft/electrons/_basis_real.py): even grid 16 x 20 x 24, Ecut 6 Ha,
+    s + p projectors on three atoms."""
+    R = np.diag([5.5, 6.5, 7.5])
+    pos = np.array([[0.1, 0.2, 0.3], [0.6, 0.55, 0.8], [0.35, 0.9, 0.1]])
+    shells = [ProjectorShell(0, 1.0), ProjectorShell(1, 0.8)]
+    D = np.stack([random_symmetric(seed, 500 + 2 * a_, 4, -1.5, 1.5) for a_ in range(3)])
+    km = ((1, 1, 1), (0.0, 0.0, 0.0))
+    k = monkhorst_pack(*km)
+    prob = Problem("tiny_gamma", R, pos, k, np.full(1, 1.0), 6.0, tuple(shape),
+                   5, 1, shells, D, None, seed, kmesh=km, extra={"real_wavefunctions": True})
+    return _finish(prob, 1.5, 1.0, 0.2)
+
+
+WORKLOADS = {"si2": si2, "si64": si64, "cu32": cu32, "tiny_fcc": tiny_fcc, "tiny_ortho": tiny_ortho,
+             "tiny_gamma": tiny_gamma}
 
 
 def get(name: str, **kw) -> Problem:

@@ -68,13 +68,14 @@ def import_reference(ref_src: str):
     return qimpy
 
 
-def build_system(qimpy, prob: wl.Problem, davidson: dict | None):
+def build_system(qimpy, prob: wl.Problem, davidson: dict | None, real: bool = False):
     from qimpy.dft import System
 
     size, offset = prob.kmesh
     el_cfg = {
         "k-mesh": {"size": list(size), "offset": list(offset), "use-inversion": False},
-        "basis": {"ke-cutoff": prob.ke_cutoff, "grid": {"shape": list(prob.grid_shape)}},
+        "basis": {"ke-cutoff": prob.ke_cutoff, "grid": {"shape": list(prob.grid_shape)},
+                  **({"real-wavefunctions": True} if real else {})},
         "fillings": {"n-bands": prob.n_bands, "n-bands-extra": prob.n_bands_extra},
         "lcao": False,
     }
@@ -244,6 +245,40 @@ def run_density_case(qimpy, name: str, full: bool, out_dir: str) -> None:
     print(f"density {name}: wrote {path}; total {rho.sum():.6f}")
 
 
+#: Gamma-point workloads with real wavefunctions (half-mesh basis)
+REAL_CASES = ("tiny_gamma",)
+
+
+def run_real_case(qimpy, name: str, out_dir: str) -> None:
+    """Reference H.psi with real wavefunctions (qimpy/dft/electrons/_basis_real.py,
+    half-mesh basis, r2c / c2r FFTs, Gweight-weighted projections): the basis
+    layout, the start vectors after the reference's constrain (padding zeroed,
+    Gz = 0 plane made Hermitian), their H.psi and <beta|psi>."""
+    import torch
+    from qimpy.dft.electrons import Wavefunction
+
+    prob = wl.get(name)
+    mine = wl.make_basis(prob.Gbasis, prob.k, prob.ke_cutoff, prob.grid_shape, real=True)
+    system = build_system(qimpy, prob, None, real=True)
+    basis = system.electrons.basis
+    assert basis.real_wavefunctions
+    assert np.array_equal(basis.n.numpy(), mine.n)
+    assert np.array_equal(basis.fft_index.numpy(), mine.fft_index)
+    beta = wl.make_projectors(prob, mine)
+    el = inject(qimpy, system, prob, beta)
+    nb = prob.n_bands + prob.n_bands_extra
+    C0 = wl.make_wavefunctions(prob, mine, nb)
+    C = Wavefunction(basis, coeff=torch.from_numpy(C0[None, :, :, None, :]).clone())
+    C.constrain()
+    C0s = C.coeff[0, :, :, 0, :].numpy().copy()
+    HC = el.hamiltonian(C).coeff[0, :, :, 0, :].numpy()
+    out = dict(n=mine.n, fft_index=mine.fft_index.astype(np.int32), C0=C0s, V_r=prob.V_r, beta=beta, hpsi=HC,
+               proj=C.proj[0].numpy(), Gweight=basis.real.Gweight.numpy())
+    path = os.path.join(out_dir, f"real_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"real {name}: wrote {path}")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
@@ -251,9 +286,10 @@ def main() -> None:
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--chefsi", action="store_true", help="only the CheFSI goldens")
     ap.add_argument("--density", action="store_true", help="only the density goldens")
+    ap.add_argument("--real", action="store_true", help="only the real-wavefunction goldens")
     args = ap.parse_args()
     qimpy = import_reference(args.ref)
-    only_part = args.chefsi or args.density
+    only_part = args.chefsi or args.density or args.real
     for name, cfg in CASES.items():
         if only_part or (args.only and name not in args.only):
             continue
@@ -266,6 +302,10 @@ def main() -> None:
         if (only_part and not args.density) or (args.only and name not in args.only):
             continue
         run_density_case(qimpy, name, full, args.out)
+    for name in REAL_CASES:
+        if (only_part and not args.real) or (args.only and name not in args.only):
+            continue
+        run_real_case(qimpy, name, args.out)
 
 
 if __name__ == "__main__":

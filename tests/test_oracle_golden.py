@@ -112,3 +112,25 @@ def test_oracle_density_matches_reference(name):
         i = g["sample_idx"]
         assert np.abs(rho[i[:, 0], i[:, 1], i[:, 2]] - g["sample"]).max() <= 1e-12 * scale
     assert np.abs(rho.sum(axis=(1, 2)) - g["plane_sums"]).max() <= 1e-12 * np.abs(g["plane_sums"]).max()
+
+
+def test_oracle_real_wavefunctions_match_reference():
+    """Gamma-point real wavefunctions (half-mesh basis, r2c/c2r FFTs, weighted
+    projections): the oracle's basis, symmetrisation, <beta|psi> and H.psi
+    against the reference run with real-wavefunctions: true."""
+    g = np.load(os.path.join(GOLDEN, "real_tiny_gamma.npz"))
+    p = wl.get("tiny_gamma")
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape, real=True)
+    assert np.array_equal(b.n, g["n"]) and np.array_equal(b.fft_index, g["fft_index"])
+    gw = oh.real_gweight(b.iG[0], int(b.n[0]), b.n_tot)
+    assert np.array_equal(gw, g["Gweight"][: b.n_tot])
+    beta = wl.make_projectors(p, b)
+    assert np.abs(beta - g["beta"]).max() <= 1e-14 * np.abs(beta).max()
+    C = wl.make_wavefunctions(p, b, p.n_bands + p.n_bands_extra)
+    oh.constrain(C, b.n)
+    oh.real_symmetrize(C, b.iG[0], p.grid_shape)
+    assert np.abs(C - g["C0"]).max() <= 1e-15 * np.abs(C).max()
+    proj = oh.project_real(beta, C, gw)
+    assert np.abs(proj - g["proj"]).max() <= 1e-12 * np.abs(g["proj"]).max()
+    HC = oh.hamiltonian_real(b.ke, p.V_r, b.fft_index, b.n, b.iG, beta, p.D_all(), C, gw)
+    assert np.abs(HC - g["hpsi"]).max() <= 1e-12 * np.abs(g["hpsi"]).max()
