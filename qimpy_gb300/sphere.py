@@ -76,14 +76,19 @@ class SphereTables:
     max_rows: int
 
 
-def build_tables(fft_index: np.ndarray, n: np.ndarray, shape, fac=None) -> SphereTables:
+def build_tables(fft_index: np.ndarray, n: np.ndarray, shape, fac=None, fft_axes=(0, 1, 2)) -> SphereTables:
+    """Sphere tables of a basis on the grid `shape` (N2 fastest).  Axes outside
+    `fft_axes` get the placeholder factorisation (N, 1) without validation:
+    the half-width z axis of a real-wavefunction grid (N2/2 + 1 complex points)
+    is transformed as a real length-N2 axis instead."""
     fft_index = np.asarray(fft_index, dtype=np.int64)
     n = np.asarray(n, dtype=np.int64)
     nk, n_tot = fft_index.shape
     N0, N1, N2 = (int(x) for x in shape)
     if max(N1, N2) >= 1 << 15:
         raise ValueError("grid too large for packed (i1, i2) indices")
-    fac = tuple(factor_axis(int(Na), None if fac is None else fac[a]) for a, Na in enumerate(shape))
+    fac = tuple((factor_axis(int(Na), None if fac is None else fac[a]) if a in fft_axes else (int(Na), 1))
+                for a, Na in enumerate(shape))
     per_k = []
     for k in range(nk):
         idx = fft_index[k, : n[k]]

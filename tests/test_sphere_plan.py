@@ -186,3 +186,52 @@ def test_density_kernel_index_replay():
                             c -= nz
                             px += 1
             assert np.all(covered == 1), (N0, N2, dtype_regs)
+
+
+def test_real_wavefunction_slab_plan_matches_oracle():
+    """Plan of the real-wavefunction (Gamma-point) local potential, replayed with
+    numpy on the half-grid sphere tables: y c2c on the slab planes
+    N1 x (N2/2+1); per y-row the x c2c, the z c2r per x-row, V on the real tile,
+    the z r2c and the x c2c; then y c2c back and the gather.  The c2r along z
+    comes last because a single z-line is not Hermitian by itself.  Must agree
+    with the oracle's irfftn/rfftn form (before its constrain)."""
+    p = wl.get("tiny_gamma")
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape, real=True)
+    N0, N1, N2 = p.grid_shape
+    N2h = N2 // 2 + 1
+    t = sp.build_tables(b.fft_index, b.n, (N0, N1, N2h), fft_axes=(0, 1))
+    (a1, a2), (b1, b2) = t.fac[0], t.fac[1]
+    C = wl.make_wavefunctions(p, b, 3)
+    oh.real_symmetrize(C, b.iG[0], p.grid_shape)
+    perm_x = sp.permutation(N0, a1, a2)
+    perm_y = sp.permutation(N1, b1, b2)
+    Vp = p.V_r[perm_x][:, perm_y]  # x, y permuted; z natural
+    k = 0
+    ns = int(t.n_slabs[k])
+    out = np.zeros_like(C)
+    for band in range(C.shape[1]):
+        planes = np.zeros((ns, N1, N2h), complex)
+        for s in range(ns):
+            P = np.zeros((N1, N2h), complex)
+            g0, g1 = t.slab_start[k, s], t.slab_start[k, s + 1]
+            v = t.yz[k, g0:g1]
+            P[v >> 16, v & 0xFFFF] = C[k, band, g0:g1]
+            planes[s] = _inv_perm(P, b1, b2, 0)  # y c2c
+        for r1 in range(N1):
+            X = np.zeros((N0, N2h), complex)
+            X[t.slab_i0[k, :ns]] = planes[:, r1, :]
+            X = _inv_perm(X, a1, a2, 0)  # x c2c
+            R = np.fft.irfft(X, n=N2, axis=1) * N2  # z c2r, unnormalised
+            R = R * Vp[:, r1, :]
+            X = np.fft.rfft(R, axis=1)  # z r2c
+            X = _fwd_perm(X, a1, a2, 0)  # x c2c back
+            planes[:, r1, :] = X[t.slab_i0[k, :ns]]
+        for s in range(ns):
+            P = _fwd_perm(planes[s], b1, b2, 0)
+            g0, g1 = t.slab_start[k, s], t.slab_start[k, s + 1]
+            v = t.yz[k, g0:g1]
+            out[k, band, g0:g1] = P[v >> 16, v & 0xFFFF] / (N0 * N1 * N2)
+    oh.constrain(out, b.n)
+    oh.real_symmetrize(out, b.iG[0], p.grid_shape)
+    want = oh.apply_potential_real(p.V_r, b.fft_index, b.n, b.iG, C)
+    assert np.abs(out - want).max() <= 1e-12 * np.abs(want).max()
