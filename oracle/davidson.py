@@ -126,6 +126,12 @@ class DavidsonResult:
     HC: np.ndarray = None  #: H C carried through the rotations (as the reference keeps it)
 
 
+def dot_real(C1: np.ndarray, C2: np.ndarray, gweight: np.ndarray) -> np.ndarray:
+    """Real-wavefunction overlap: Re sum_G w_G conj(C1) C2 (the implicit -G
+    partners), imaginary part zeroed (qimpy/dft/electrons/_wavefunction_dot.py:55-88)."""
+    return np.matmul(C1.conj() * gweight, np.swapaxes(C2, 1, 2)).real.astype(np.complex128)
+
+
 def davidson(
     hamiltonian: Callable[[np.ndarray], np.ndarray],
     C: np.ndarray,
@@ -134,9 +140,21 @@ def davidson(
     n_bands: int,
     n_iterations: int = 100,
     eig_threshold: float = 1e-8,
+    gweight: np.ndarray | None = None,
+    symmetrize: Callable[[np.ndarray], np.ndarray] | None = None,
 ) -> DavidsonResult:
     """Block Davidson (qimpy/dft/electrons/_davidson.py:141-235) on orthonormal
-    start vectors C[k, n_bands + n_bands_extra, g]."""
+    start vectors C[k, n_bands + n_bands_extra, g].
+
+    Real (Gamma-point) wavefunctions: `gweight` (1 on Gz = 0, 2 elsewhere, 0 on
+    padding) weights the overlaps, norms and kinetic energies and `symmetrize`
+    makes the Gz = 0 plane Hermitian in constrain (_wavefunction.py:226-275)."""
+    if gweight is not None:
+        dot_, band_norm_ = (lambda A, B: dot_real(A, B, gweight)), \
+            (lambda A: np.sqrt(((np.square(A.real) + np.square(A.imag)) * gweight).sum(axis=-1)))
+        band_ke_ = lambda A, kin: band_ke(A, kin * gweight)  # noqa: E731
+    else:
+        dot_, band_norm_, band_ke_ = dot, band_norm, band_ke
     nk, n_bands_max, n_tot = C.shape
     if 2 * n_bands_max >= int(n.min()):
         raise ValueError(
@@ -145,7 +163,7 @@ def davidson(
     norm_cut = np.sqrt(n_tot * 1e-15)  # _davidson.py:56-58
     hpsi_bands = nk * n_bands_max
     HC = hamiltonian(C)
-    eig, V = eigh(dot(C, HC))  # _davidson.py:164-168
+    eig, V = eigh(dot_(C, HC))  # _davidson.py:164-168
     C = matmul(C, V)
     HC = matmul(HC, V)
     n_eigs_done = 0
@@ -157,23 +175,29 @@ def davidson(
         eig_sel = eig[:, n_eigs_done:, None]
         C_sel = C[:, n_eigs_done:]
         HC_sel = HC[:, n_eigs_done:]
-        KEref = band_ke(C_sel, ke)
+        KEref = band_ke_(C_sel, ke)
         Cexp = precondition(HC_sel - C_sel * eig_sel, ke, KEref)
-        norm_exp = band_norm(Cexp)
+        norm_exp = band_norm_(Cexp)
         low_k, low_b = np.where(norm_exp < norm_cut)  # _davidson.py:101-115
         if len(low_k):
+            # Real wavefunctions draw the same numbers: the reference's extra
+            # conjugate-seeded Gz = 0 term (_wavefunction_init.py:175-181) is added
+            # to an advanced-indexing copy and does not reach the coefficients;
+            # the Hermitian symmetrisation of constrain below follows.
             randomize_selected(Cexp, low_k, low_b, i_iter, n, int(n.max()), nk, ke)
             norm_exp[low_k, low_b] = 1.0
         Cexp = Cexp * (1.0 / norm_exp)[..., None]
         for k in range(nk):
             Cexp[k, :, int(n[k]) :] = 0.0
+        if symmetrize is not None:
+            symmetrize(Cexp)
         n_bands_exp = Cexp.shape[1]
         n_bands_new = n_bands_cur + n_bands_exp
         Cnew = np.concatenate((C, Cexp), axis=1)
-        C_OC_new = tile_expansion(np.eye(n_bands_cur)[None], dot(Cnew, Cexp))
+        C_OC_new = tile_expansion(np.eye(n_bands_cur)[None], dot_(Cnew, Cexp))
         HCexp = hamiltonian(Cexp)
         hpsi_bands += nk * n_bands_exp
-        C_HC_new = tile_expansion(np.stack([np.diag(e) for e in eig]), dot(Cnew, HCexp))
+        C_HC_new = tile_expansion(np.stack([np.diag(e) for e in eig]), dot_(Cnew, HCexp))
         eig_new, V_new = eighg(C_HC_new, C_OC_new)
         n_bands_next = min(n_bands_new, n_bands_max)
         V_new = V_new[..., :n_bands_next]

@@ -274,6 +274,15 @@ def run_real_case(qimpy, name: str, out_dir: str) -> None:
     HC = el.hamiltonian(C).coeff[0, :, :, 0, :].numpy()
     out = dict(n=mine.n, fft_index=mine.fft_index.astype(np.int32), C0=C0s, V_r=prob.V_r, beta=beta, hpsi=HC,
                proj=C.proj[0].numpy(), Gweight=basis.real.Gweight.numpy())
+    # Davidson with real wavefunctions from the orthonormalised, symmetrised start vectors.
+    from qimpy.dft.electrons import Davidson
+
+    el.C = Wavefunction(basis, coeff=torch.from_numpy(C0s[None, :, :, None, :]).clone()).orthonormalize()
+    el.deig_max = np.inf
+    solver = Davidson(electrons=el, n_iterations=200, eig_threshold=1e-12)
+    solver()
+    out.update(eig=el.eig[0].numpy().copy(), davidson_iterations=np.int64(solver._i_iter),
+               eig_threshold=np.float64(1e-12))
     path = os.path.join(out_dir, f"real_{name}.npz")
     np.savez_compressed(path, **out)
     print(f"real {name}: wrote {path}")
