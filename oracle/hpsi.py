@@ -155,3 +155,19 @@ def hamiltonian_real(ke, V_r, fft_index, n, iG, beta, D_all, C, gweight) -> np.n
     if beta is not None and beta.shape[1]:
         HC += apply_nonlocal(beta, D_all, project_real(beta, C, gweight))
     return HC
+
+
+def collect_density_real(fft_index: np.ndarray, shape, C: np.ndarray, prefac: np.ndarray) -> np.ndarray:
+    """Density of real (Gamma-point) wavefunctions: psi = irfft(scatter(C)) on
+    the half grid (no scaling), rho = sum_b prefac |psi|^2 (_basis_ops.py:207-296
+    with the real-basis expand of _basis_ops.py:119-163)."""
+    nk, nb, n_tot = C.shape
+    half = (shape[0], shape[1], shape[2] // 2 + 1)
+    rho = np.zeros(tuple(shape))
+    for k in range(nk):
+        grid = np.zeros((nb, int(np.prod(half))), dtype=np.complex128)
+        grid[:, fft_index[k]] = C[k]
+        psi_r = sfft.irfftn(grid.reshape((nb,) + half), s=tuple(shape), axes=(1, 2, 3), norm="forward",
+                            workers=_WORKERS)
+        rho += np.einsum("b,bxyz->xyz", prefac[k], psi_r ** 2)
+    return rho

@@ -274,6 +274,11 @@ def run_real_case(qimpy, name: str, out_dir: str) -> None:
     HC = el.hamiltonian(C).coeff[0, :, :, 0, :].numpy()
     out = dict(n=mine.n, fft_index=mine.fft_index.astype(np.int32), C0=C0s, V_r=prob.V_r, beta=beta, hpsi=HC,
                proj=C.proj[0].numpy(), Gweight=basis.real.Gweight.numpy())
+    # Density of the symmetrised start vectors with seeded fillings (c2r expand).
+    f = wl.make_fillings(prob, nb)
+    Cd = Wavefunction(basis, coeff=torch.from_numpy(C0s[None, :, :, None, :]).clone())
+    out.update(f=f, rho=basis.collect_density(Cd, torch.from_numpy(f)[None].clone(), False).data[0].numpy(),
+               w_sk=basis.w_sk.numpy().reshape(-1).copy(), volume=np.float64(system.lattice.volume))
     # Davidson with real wavefunctions from the orthonormalised, symmetrised start vectors.
     from qimpy.dft.electrons import Davidson
 

@@ -161,3 +161,12 @@ def test_oracle_real_wavefunction_davidson_matches_reference():
     Cc = od.orthonormalize(wl.make_wavefunctions(p, bc, p.n_bands + p.n_bands_extra))
     rc = od.davidson(Hc, Cc, bc.ke, bc.n, p.n_bands, 200, 1e-12)
     assert np.abs(rc.eig[:, : p.n_bands] - g["eig"][:, : p.n_bands]).max() < 1e-9
+
+
+def test_oracle_real_wavefunction_density_matches_reference():
+    g = np.load(os.path.join(GOLDEN, "real_tiny_gamma.npz"))
+    p = wl.get("tiny_gamma")
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape, real=True)
+    assert np.allclose(g["w_sk"], 2.0 * p.wk)
+    rho = oh.collect_density_real(b.fft_index, p.grid_shape, g["C0"], g["f"] * (2.0 * p.wk[:, None] / p.volume))
+    assert np.abs(rho - g["rho"]).max() <= 1e-12 * np.abs(g["rho"]).max()
