@@ -19,9 +19,14 @@ from . import davidson as od
 
 def chefsi(hamiltonian: Callable[[np.ndarray], np.ndarray], C: np.ndarray, ke: np.ndarray, n: np.ndarray,
            n_bands: int, ke_cutoff: float, V_max: float, n_iterations: int = 100, eig_threshold: float = 1e-8,
-           filter_order: int = 10, init_threshold: float = 1e-1) -> od.DavidsonResult:
-    """CheFSI from orthonormal start vectors C[k, n_bands + n_bands_extra, g]."""
-    warm = od.davidson(hamiltonian, C, ke, n, n_bands, n_iterations, init_threshold)  # _chefsi.py:86-92
+           filter_order: int = 10, init_threshold: float = 1e-1, gweight: np.ndarray | None = None,
+           symmetrize=None) -> od.DavidsonResult:
+    """CheFSI from orthonormal start vectors C[k, n_bands + n_bands_extra, g];
+    `gweight` / `symmetrize` for real (Gamma-point) wavefunctions as in
+    oracle.davidson.davidson."""
+    dot_ = od.dot if gweight is None else (lambda A, B: od.dot_real(A, B, gweight))
+    warm = od.davidson(hamiltonian, C, ke, n, n_bands, n_iterations, init_threshold,
+                       gweight=gweight, symmetrize=symmetrize)  # _chefsi.py:86-92
     C, HC, eig = warm.C, warm.HC, warm.eig
     hpsi_bands = warm.hpsi_bands
     nk = C.shape[0]
@@ -51,7 +56,7 @@ def chefsi(hamiltonian: Callable[[np.ndarray], np.ndarray], C: np.ndarray, ke: n
         C = np.concatenate((C0, Y), axis=1)
         HC = np.concatenate((HC0, HY), axis=1)
         eig_prev = eig
-        eig, V = od.eighg(od.dot(C, HC), od.dot(C, C))  # _chefsi.py:157-161
+        eig, V = od.eighg(dot_(C, HC), dot_(C, C))  # _chefsi.py:157-161
         C = od.matmul(C, V)
         HC = od.matmul(HC, V)
         deig = np.abs(eig - eig_prev)[:, :n_bands]  # _check_deig, _davidson.py:126-139

@@ -288,6 +288,14 @@ def run_real_case(qimpy, name: str, out_dir: str) -> None:
     solver()
     out.update(eig=el.eig[0].numpy().copy(), davidson_iterations=np.int64(solver._i_iter),
                eig_threshold=np.float64(1e-12))
+    # CheFSI with real wavefunctions from the same start.
+    from qimpy.dft.electrons import CheFSI
+
+    el.C = Wavefunction(basis, coeff=torch.from_numpy(C0s[None, :, :, None, :]).clone()).orthonormalize()
+    el.deig_max = np.inf
+    cf = CheFSI(electrons=el, n_iterations=100, eig_threshold=1e-11, filter_order=10, init_threshold=1e-1)
+    cf()
+    out.update(chefsi_eig=el.eig[0].numpy().copy(), chefsi_iterations=np.int64(cf._i_iter))
     path = os.path.join(out_dir, f"real_{name}.npz")
     np.savez_compressed(path, **out)
     print(f"real {name}: wrote {path}")

@@ -170,3 +170,22 @@ def test_oracle_real_wavefunction_density_matches_reference():
     assert np.allclose(g["w_sk"], 2.0 * p.wk)
     rho = oh.collect_density_real(b.fft_index, p.grid_shape, g["C0"], g["f"] * (2.0 * p.wk[:, None] / p.volume))
     assert np.abs(rho - g["rho"]).max() <= 1e-12 * np.abs(g["rho"]).max()
+
+
+def test_oracle_real_wavefunction_chefsi_matches_reference():
+    from oracle import chefsi as oc
+
+    g = np.load(os.path.join(GOLDEN, "real_tiny_gamma.npz"))
+    p = wl.get("tiny_gamma")
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape, real=True)
+    gw = oh.real_gweight(b.iG[0], int(b.n[0]), b.n_tot)
+    beta = wl.make_projectors(p, b)
+    H = lambda X: oh.hamiltonian_real(b.ke, p.V_r, b.fft_index, b.n, b.iG, beta, p.D_all(), X, gw)  # noqa: E731
+    sym = lambda X: oh.real_symmetrize(X, b.iG[0], p.grid_shape)  # noqa: E731
+    C = g["C0"].copy()
+    C = od.matmul(C, od.ortho_matrix(od.dot_real(C, C, gw)))
+    r = oc.chefsi(H, C, b.ke, b.n, p.n_bands, p.ke_cutoff, float(p.V_r.max()), 100, 1e-11, 10, 1e-1,
+                  gweight=gw, symmetrize=sym)
+    assert r.converged
+    assert np.abs(r.eig[:, : p.n_bands] - g["chefsi_eig"][:, : p.n_bands]).max() < 1e-10
+    assert r.iterations == int(g["chefsi_iterations"])
