@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define QGB_ABI_VERSION 1
+#define QGB_ABI_VERSION 2
 
 enum qgb_dtype { QGB_F64 = 0, QGB_F32 = 1 };
 
@@ -155,7 +155,9 @@ int qgb_apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out
  * calls no allocator.
  *   - The first call on a device looks up the array's device address (once per
  *     device, with that device current); make that first call before any
- *     stream capture.
+ *     stream capture.  A device reset (cudaDeviceReset) gives the device a
+ *     new context and the array a new address: the first call after it looks
+ *     the address up again, so it too belongs before any capture.
  *   - All calls share the one array and it keeps the previous call's contents;
  *     nothing in it needs to start at zero (every plane is written before it is
  *     read within a call).  Calls that overlap on the GPU (different streams,
@@ -204,10 +206,34 @@ int qgb_apply_potential_batched(const qgb_batch_item* items, int n_items, const 
 /*
  * projT[k][b][p] = sum_g conj(beta[k][p][g]) C[k][b][g]  (replaces Wavefunction.proj
  * = beta ^ C, qimpy/dft/electrons/_wavefunction.py:106-123 and
- * _wavefunction_dot.py:18-107).
+ * _wavefunction_dot.py:18-107).  The sum over the basis is split across CTAs;
+ * `workspace` holds the partial sums (qgb_project_workspace_bytes, may be 0),
+ * added in a fixed order, so results are reproducible bit for bit.
  */
+size_t qgb_project_workspace_bytes(int dtype, int nk, int P, int nb, int n_tot);
 int qgb_project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb,
-                int n_tot, void* stream);
+                int n_tot, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Overlaps of two band blocks at every k: out[k][i][j] = sum_g conj(X[k][i][g])
+ * Y[k][j][g] for X [nk][nx][n_tot], Y [nk][ny][n_tot] of `dtype`; out is
+ * complex128 [nk][nx][ny] for both dtypes (FP32 inputs: FP32 partial sums,
+ * added in FP64).  Replaces Wavefunction.dot / ^ for one spin and no spinors
+ * (qimpy/dft/electrons/_wavefunction_dot.py:18-107).  Workspace of
+ * qgb_dot_workspace_bytes (split-K partials, fixed summation order).
+ */
+size_t qgb_dot_workspace_bytes(int dtype, int nk, int nx, int ny, int n_tot);
+int qgb_dot(int dtype, const void* X, int nx, const void* Y, int ny, int nk, int n_tot, void* out,
+            void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Band rotation out[k][j][g] = sum_i M[k][i][j] C[k][i][g] (+= with
+ * QGB_ACCUMULATE) for C [nk][n_in][n_tot], M [nk][n_in][n_out] and out
+ * [nk][n_out][n_tot], all of `dtype`; out must not alias C.  Replaces
+ * Wavefunction.matmul / @ (qimpy/dft/electrons/_wavefunction_dot.py:137-191).
+ */
+int qgb_matmul(int dtype, const void* C, int n_in, int nk, int n_tot, const void* M, int n_out, void* out,
+               unsigned flags, void* stream);
 
 /*
  * out[k][b][g] += sum_p beta[k][p][g] (D_all projT[k][b])[p]  (replaces
@@ -222,15 +248,45 @@ int qgb_apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, 
 /*
  * HC = KE C + V C + beta D <beta|C>  (replaces Electrons.hamiltonian,
  * qimpy/dft/electrons/_hamiltonian.py:7-29, for a fixed local potential).
- * projT receives <beta|C> (the reference caches it as C.proj).  Workspace:
- * qgb_potential_workspace_bytes + nk*nb*P complex values.  beta may be NULL
- * when P == 0.
+ * projT receives <beta|C> (the reference caches it as C.proj).  Workspace of
+ * qgb_hamiltonian_workspace_bytes: the slab planes, D <beta|C> and the
+ * projection's partial sums.  beta may be NULL when P == 0.
  */
 int qgb_hamiltonian(const qgb_sphere* s, int dtype, const void* C, void* HC, int nb,
                     const void* beta, const void* D, int n_atoms, int pa, void* projT,
                     void* workspace, size_t workspace_bytes, void* stream);
 
 size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int dtype);
+
+/*
+ * Band-wise passes of the Davidson iteration (one read of the bands each; FP64
+ * sums; C and HC of `dtype`, [nk][nb_all][n_tot], the pass covers bands
+ * [b0, b0 + nb); ke FP64 [nk][n_tot]; per-band results FP64 [nk][nb]):
+ *
+ * qgb_band_norm_ke: norm = ||C_b||, band_ke = sum_g |C_bg|^2 KE_g (either may be
+ *   NULL; ke may be NULL without band_ke).  Replaces Wavefunction.band_norm and
+ *   band_ke (qimpy/dft/electrons/_wavefunction.py:226-247).
+ * qgb_residual: R = HC_b - eig[k][b0 + b] C_b (eig FP64 [nk][eig_ld]); with
+ *   KEref (FP64 [nk][nb]) preconditioned as R / (x + exp(-x)), x = KE / KEref_b;
+ *   stored to out [nk][nb][n_tot] (may be NULL) and reduced to norm (may be
+ *   NULL).  Replaces the residual and Davidson.precondition
+ *   (qimpy/dft/electrons/_davidson.py:92-99, 177-180).
+ * qgb_normalize_bands: X [nk][nb][n_tot] in place: bands with norm < norm_cut
+ *   are re-randomised with the reference's seeded generator (state (1 + seed)
+ *   + g + n_max (b + nb k), one discarded draw, Box-Muller, damped by
+ *   1 / (1 + (4/3 KE)^6), inside the sphere n[k]) and their norm set to 1; the
+ *   others are divided by their norm; padding zeroed.  Replaces
+ *   Davidson._regularize with Wavefunction.randomize_selected and the
+ *   normalisation and constrain that follow (_davidson.py:101-115, 181-183;
+ *   _wavefunction_init.py:127-188; _wavefunction.py:264-275).  n: int32 [nk].
+ */
+int qgb_band_norm_ke(int dtype, const void* C, int nb_all, int b0, int nb, int nk, int n_tot, const double* ke,
+                     double* norm, double* band_ke, void* stream);
+int qgb_residual(int dtype, const void* HC, const void* C, int nb_all, int b0, int nb, int nk, int n_tot,
+                 const double* eig, int eig_ld, const double* ke, const double* KEref, void* out, double* norm,
+                 void* stream);
+int qgb_normalize_bands(int dtype, void* X, int nb, int nk, int n_tot, const int32_t* n, double* norm,
+                        double norm_cut, long long seed, long long n_max, const double* ke, void* stream);
 
 /*
  * Mixed-precision nonlocal term on the tcgen05 tensor cores (split-BF16x3,
@@ -274,16 +330,6 @@ int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, 
                           int* dev_error, void* stream);
 
 /*
- * The underlying real GEMM, exposed for verification: D (FP32 [M][N], N <= 64)
- * = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with bf16 K-major A [M][lda],
- * B [N][ldb] (lda, ldb multiples of 8).  workspace >= ceil(M/128)*128*64*4 B.
- * No reference counterpart (test aid for the tensor-core path).
- */
-int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N,
-                       int K, int lda, int ldb, float* D, int* dev_error, void* workspace,
-                       size_t workspace_bytes, void* stream);
-
-/*
  * FP64 eigenpairs of nk Hermitian n x n matrices A ([nk][n][n] complex128,
  * row-major) in one batched cuSOLVER call on `stream`: W [nk][n] ascending
  * eigenvalues; A is overwritten with V^H (row j = conj of eigenvector j);
@@ -295,15 +341,6 @@ int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, con
 size_t qgb_subspace_eigh_workspace_bytes(int64_t nk, int64_t n);
 int qgb_subspace_eigh(void* A, double* W, int* info, int64_t nk, int64_t n, void* workspace,
                       size_t workspace_bytes, void* stream);
-
-/*
- * Diagnostic: `blocks` x `threads` threads each run 8 independent FMA chains
- * of 8*iters steps (64*iters FMAs = 128*iters flops per thread).  Timed by
- * the caller; gives the FP64/FP32 CUDA-core peak used as a roofline
- * denominator.  `out` receives nothing in practice (needs `blocks` reals).
- * No reference counterpart (measurement aid).
- */
-int qgb_fma_burn(int dtype, int blocks, int threads, int iters, void* out, void* stream);
 
 #ifdef __cplusplus
 }

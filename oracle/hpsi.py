@@ -48,7 +48,8 @@ def apply_potential(V_r: np.ndarray, fft_index: np.ndarray, n: np.ndarray, C: np
         grid = np.zeros((nb, N), dtype=np.complex128)
         grid[:, fft_index[k]] = C[k]
         psi_r = sfft.ifftn(grid.reshape((nb,) + shape), axes=(1, 2, 3), norm="forward", workers=_WORKERS)
-        psi_r *= V_r[None]
+        # real V times complex psi, as pairs of doubles (one pass, no complex promotion of V)
+        psi_r.view(np.float64).reshape(psi_r.shape + (2,))[...] *= V_r[None, ..., None]
         VC = sfft.fftn(psi_r, axes=(1, 2, 3), norm="forward", workers=_WORKERS).reshape(nb, N)
         out[k] = VC[:, fft_index[k]]
     return constrain(out, n)
@@ -56,8 +57,13 @@ def apply_potential(V_r: np.ndarray, fft_index: np.ndarray, n: np.ndarray, C: np
 
 def project(beta: np.ndarray, C: np.ndarray) -> np.ndarray:
     """<beta|C>: proj[k, p, b] = sum_g conj(beta[k, p, g]) C[k, b, g]
-    (qimpy/dft/electrons/_wavefunction.py:106-123 via _wavefunction_dot.py:18-107)."""
-    return np.matmul(beta.conj(), np.swapaxes(C, 1, 2))
+    (qimpy/dft/electrons/_wavefunction.py:106-123 via _wavefunction_dot.py:18-107),
+    evaluated as conj(beta[k] @ conj(C[k])^T) so that only the band block is
+    conjugated (one BLAS product per k)."""
+    out = np.empty((beta.shape[0], beta.shape[1], C.shape[1]), dtype=np.result_type(beta, C))
+    for k in range(beta.shape[0]):
+        out[k] = np.conj(beta[k] @ np.conj(C[k]).T)
+    return out
 
 
 def apply_nonlocal(beta: np.ndarray, D_all: np.ndarray, proj: np.ndarray) -> np.ndarray:

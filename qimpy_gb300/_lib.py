@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(PKG, "libqimpy_gb300_debug.so" if DEBUG else "libqimpy_g
 
 QGB_F64, QGB_F32 = 0, 1
 QGB_ADD_KE, QGB_ACCUMULATE = 1, 2
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 _ERRORS = {1: "invalid argument", 2: "workspace too small", 3: "CUDA error", 4: "cuBLAS error",
            5: "unsupported", 6: "cuSOLVER error"}
@@ -57,14 +57,26 @@ _SIGS = {
     "qgb_apply_ke": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p]),
     "qgb_apply_potential": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
                                        ct.c_uint, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_project_workspace_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int]),
     "qgb_project": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int,
-                               ct.c_int, ct.c_void_p]),
+                               ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_dot_workspace_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int]),
+    "qgb_dot": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p,
+                           ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_band_norm_ke": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
+                                    ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "qgb_residual": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
+                                ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                ct.c_void_p]),
+    "qgb_normalize_bands": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                       ct.c_double, ct.c_longlong, ct.c_longlong, ct.c_void_p, ct.c_void_p]),
+    "qgb_matmul": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int,
+                              ct.c_void_p, ct.c_uint, ct.c_void_p]),
     "qgb_apply_nonlocal": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p,
                                       ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
     "qgb_hamiltonian": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
                                    ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
                                    ct.c_size_t, ct.c_void_p]),
-    "qgb_fma_burn": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
     "qgb_apply_potential_static": (ct.c_int, [ct.POINTER(QgbSphere), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
                                               ct.c_uint, ct.c_void_p]),
     "qgb_static_scratch_bytes": (ct.c_size_t, []),
@@ -91,13 +103,40 @@ _SIGS = {
     "qgb_subspace_eigh_workspace_bytes": (ct.c_size_t, [ct.c_int64, ct.c_int64]),
     "qgb_subspace_eigh": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64, ct.c_void_p,
                                      ct.c_size_t, ct.c_void_p]),
-    "qgb_tc_gemm_bf16x3": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
-                                      ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
-                                      ct.c_size_t, ct.c_void_p]),
 }
 
 #: Every symbol the header declares (checked by the CPU tests).
 EXPORTED = tuple(_SIGS)
+
+#: Measurement and test aids of libqimpy_gb300_aux.so (include/qimpy_gb300_aux.h).
+AUX_PATH = os.path.join(PKG, "libqimpy_gb300_aux.so")
+_AUX_SIGS = {
+    "qgb_fma_burn": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "qgb_tc_gemm_bf16x3": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
+                                      ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                      ct.c_size_t, ct.c_void_p]),
+    "qgb_tc_wait_timeout_test": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_ulonglong, ct.c_void_p]),
+}
+AUX_EXPORTED = tuple(_AUX_SIGS)
+_aux = None
+
+
+def aux() -> ct.CDLL:
+    """The auxiliary library of measurement and test aids (loads the main one first)."""
+    global _aux
+    lib()
+    if _aux is None:
+        with _lock:
+            if _aux is None:
+                if not os.path.exists(AUX_PATH):
+                    raise RuntimeError(f"{AUX_PATH} is missing: build it with `python -m qimpy_gb300.build`")
+                handle = ct.CDLL(AUX_PATH)
+                for name, (res, args) in _AUX_SIGS.items():
+                    fn = getattr(handle, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                _aux = handle
+    return _aux
 
 
 def lib() -> ct.CDLL:

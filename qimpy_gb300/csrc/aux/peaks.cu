@@ -1,6 +1,6 @@
 // FMA-pipe throughput probe: the FP64 / FP32 CUDA-core roofline denominators
 // (the measured-peaks file records only HBM copy and bf16 tensor rates).
-#include "qgb_common.cuh"
+#include "../qgb_common.cuh"
 
 namespace qgb {
 

@@ -1,8 +1,11 @@
 // extern "C" entry points of libqimpy_gb300 (declared in include/qimpy_gb300.h).
 #include <cstdarg>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <string>
 #include <unordered_map>
+#include <utility>
 
 #include "qgb_common.cuh"
 
@@ -29,13 +32,34 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+int raise_smem_limit(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> raised;
+  int dev = 0;
+  QGB_CUDA_CHECK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& have = raised[{kernel, dev}];
+  if (bytes <= have) return QGB_OK;
+  QGB_CUDA_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+  have = bytes;
+  return QGB_OK;
+}
+
 int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true);
 size_t plane_bytes_per_band(const qgb_sphere& s, int dtype);
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
                     void* ws, size_t ws_bytes, cudaStream_t st);
 int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, cudaStream_t st);
-int project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb, int n_tot,
-            cudaStream_t st);
+size_t project_workspace_bytes(int dtype, int nk, int P, int nb, int n_tot);
+int project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb, int n_tot, void* ws,
+            size_t ws_bytes, cudaStream_t st);
+size_t gram_workspace_bytes(int dtype, int nk, int M, int N, int K);
+int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, const void* B, long long b_batch,
+         int ldb, int nk, int M, int N, int K, void* out, long long out_batch, int oi, int oj, void* ws,
+         size_t ws_bytes, cudaStream_t st);
+int rotate(int dtype, const void* X, long long x_batch, int ldx, const void* W, long long w_batch, int wi, int wj,
+           int nk, int Kin, int Nout, int G, void* out, long long out_batch, int ldo, bool accumulate,
+           cudaStream_t st);
 int apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int pa, const void* projT,
                    void* out, int nk, int nb, int n_tot, void* work, cudaStream_t st);
 #ifdef QGB_DEBUG_CHECKS
@@ -81,8 +105,6 @@ static int side_stream(SideStream* out) {
   *out = it->second;
   return QGB_OK;
 }
-int tc_gemm_test(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N, int K,
-                 int lda, int ldb, float* D, int* err, void* ws, size_t ws_bytes, cudaStream_t st);
 
 }  // namespace qgb
 
@@ -99,11 +121,19 @@ size_t qgb_potential_workspace_bytes(const qgb_sphere* s, int nb, int dtype) {
   return plane_bytes_per_band(*s, dtype) * static_cast<size_t>(nb);
 }
 
+static inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Workspace of qgb_hamiltonian: [D proj (nk nb P complex) | <beta|psi> split-K
+// partials | slab planes], each part 256-byte aligned.
+static size_t ham_nonlocal_bytes(const qgb_sphere& s, int nb, int P, int dtype) {
+  if (P == 0 || nb == 0) return 0;
+  return align256(static_cast<size_t>(s.nk) * nb * P * elem_bytes(dtype)) +
+         align256(project_workspace_bytes(dtype, s.nk, P, nb, s.n_tot));
+}
+
 size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int dtype) {
   if (!s || nb < 0 || P < 0) return 0;
-  const size_t nl = static_cast<size_t>(s->nk) * nb * P * elem_bytes(dtype);
-  const size_t nl_aligned = (nl + 255) / 256 * 256;
-  return nl_aligned + plane_bytes_per_band(*s, dtype) * static_cast<size_t>(nb);
+  return ham_nonlocal_bytes(*s, nb, P, dtype) + plane_bytes_per_band(*s, dtype) * static_cast<size_t>(nb);
 }
 
 int qgb_permute_real_space(const qgb_sphere* s, int32_t* perm) {
@@ -128,10 +158,42 @@ int qgb_apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out
                          static_cast<cudaStream_t>(stream));
 }
 
+size_t qgb_project_workspace_bytes(int dtype, int nk, int P, int nb, int n_tot) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return 0;
+  return project_workspace_bytes(dtype, nk, P, nb, n_tot);
+}
+
 int qgb_project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb, int n_tot,
-                void* stream) {
+                void* workspace, size_t workspace_bytes, void* stream) {
   if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
-  return project(dtype, beta, C, projT, nk, P, nb, n_tot, static_cast<cudaStream_t>(stream));
+  return project(dtype, beta, C, projT, nk, P, nb, n_tot, workspace, workspace_bytes,
+                 static_cast<cudaStream_t>(stream));
+}
+
+size_t qgb_dot_workspace_bytes(int dtype, int nk, int nx, int ny, int n_tot) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return 0;
+  return gram_workspace_bytes(dtype, nk, nx, ny, n_tot);
+}
+
+int qgb_dot(int dtype, const void* X, int nx, const void* Y, int ny, int nk, int n_tot, void* out, void* workspace,
+            size_t workspace_bytes, void* stream) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
+  if (nk < 0 || nx < 0 || ny < 0 || n_tot < 1) return fail(QGB_ERR_INVALID, "bad dot sizes");
+  return gram(dtype, QGB_F64, X, static_cast<long long>(nx) * n_tot, n_tot, Y, static_cast<long long>(ny) * n_tot,
+              n_tot, nk, nx, ny, n_tot, out, static_cast<long long>(nx) * ny, ny, 1, workspace, workspace_bytes,
+              static_cast<cudaStream_t>(stream));
+}
+
+int qgb_matmul(int dtype, const void* C, int n_in, int nk, int n_tot, const void* M, int n_out, void* out,
+               unsigned flags, void* stream) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
+  if (nk < 0 || n_in < 0 || n_out < 0 || n_tot < 1) return fail(QGB_ERR_INVALID, "bad matmul sizes");
+  if (flags & ~QGB_ACCUMULATE) return fail(QGB_ERR_INVALID, "unknown matmul flags 0x%x", flags);
+  if (n_in > 0 && C != nullptr && C == out) return fail(QGB_ERR_INVALID, "C and out must not alias");
+  // out[k][j][g] = sum_i M[k][i][j] C[k][i][g]: W(i, j) = M[i*n_out + j].
+  return rotate(dtype, C, static_cast<long long>(n_in) * n_tot, n_tot, M, static_cast<long long>(n_in) * n_out,
+                n_out, 1, nk, n_in, n_out, n_tot, out, static_cast<long long>(n_out) * n_tot, n_tot,
+                (flags & QGB_ACCUMULATE) != 0, static_cast<cudaStream_t>(stream));
 }
 
 int qgb_apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int pa, const void* projT,
@@ -147,17 +209,18 @@ int qgb_hamiltonian(const qgb_sphere* s, int dtype, const void* C, void* HC, int
   int rc = validate_sphere(s, dtype);
   if (rc) return rc;
   if (C == HC) return fail(QGB_ERR_INVALID, "C and HC must not alias");
+  if (n_atoms < 0 || pa < 0 || nb < 0) return fail(QGB_ERR_INVALID, "bad nonlocal sizes");
   const int P = n_atoms * pa;
-  const size_t nl = static_cast<size_t>(s->nk) * nb * P * elem_bytes(dtype);
-  const size_t nl_aligned = (nl + 255) / 256 * 256;
-  if (workspace_bytes < nl_aligned) return fail(QGB_ERR_WORKSPACE, "workspace too small for nonlocal term");
+  const size_t nl = ham_nonlocal_bytes(*s, nb, P, dtype);
+  if (workspace_bytes < nl) return fail(QGB_ERR_WORKSPACE, "workspace too small for nonlocal term");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   char* ws = static_cast<char*>(workspace);
-  rc = apply_potential(s, dtype, C, HC, nb, QGB_ADD_KE, ws + nl_aligned, workspace_bytes - nl_aligned, st);
+  rc = apply_potential(s, dtype, C, HC, nb, QGB_ADD_KE, ws + nl, workspace_bytes - nl, st);
   if (rc) return rc;
-  if (P > 0) {
+  if (P > 0 && nb > 0) {
     if (!projT) return fail(QGB_ERR_INVALID, "projT is NULL with P > 0");
-    rc = project(dtype, beta, C, projT, s->nk, P, nb, s->n_tot, st);
+    const size_t dp = align256(static_cast<size_t>(s->nk) * nb * P * elem_bytes(dtype));
+    rc = project(dtype, beta, C, projT, s->nk, P, nb, s->n_tot, ws + dp, nl - dp, st);
     if (rc) return rc;
     rc = apply_nonlocal(dtype, beta, D, n_atoms, pa, projT, HC, s->nk, nb, s->n_tot, ws, st);
     if (rc) return rc;
@@ -246,11 +309,5 @@ int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, 
   return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl, dev_error, 2, st);
 }
 
-int qgb_tc_gemm_bf16x3(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo, int M, int N,
-                       int K, int lda, int ldb, float* D, int* dev_error, void* workspace, size_t workspace_bytes,
-                       void* stream) {
-  return tc_gemm_test(a_hi, a_lo, b_hi, b_lo, M, N, K, lda, ldb, D, dev_error, workspace, workspace_bytes,
-                      static_cast<cudaStream_t>(stream));
-}
 
 }  // extern "C"

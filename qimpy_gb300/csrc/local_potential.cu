@@ -623,23 +623,11 @@ size_t plane_bytes_per_band(const qgb_sphere& s, int dtype) {
   return static_cast<size_t>(s.nk) * s.max_slabs * s.N[1] * s.N[2] * elem_bytes(dtype);
 }
 
-// Kernels' shared-memory limits are raised lazily, to the largest size asked
-// for so far; the check and the raise are one step under this lock, so that
-// host threads launching for different grids cannot lower a limit another
-// thread is about to launch with.
-static std::mutex g_attr_mu;
-
+// Kernels' shared-memory limits are raised lazily (raise_smem_limit: per
+// kernel and device, to the largest size asked for so far).
 static int launch_xpass_async(const qgb_sphere& s, const LocalParams& lp, float2* planes, cudaStream_t st) {
-  static size_t configured = 0;
   const size_t smx = xpass_async_smem_bytes(s);
-  {
-    std::lock_guard<std::mutex> lock(g_attr_mu);
-    if (smx > configured) {
-      QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_async<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smx));
-      configured = smx;
-    }
-  }
+  if (int rc = raise_smem_limit(k_xpass_async<float>, smx)) return rc;
   const dim3 g2(s.N[1], lp.nb, s.nk);
   k_xpass_async<float><<<g2, kThreads, smx, st>>>(s, lp, planes);
   QGB_LAUNCH_CHECK("k_xpass_async");
@@ -669,14 +657,10 @@ static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* 
 
 template <typename T>
 static int set_smem_limits(size_t smem) {
-  static size_t configured = 0;
-  std::lock_guard<std::mutex> lock(g_attr_mu);
-  if (smem <= configured) return QGB_OK;
-  QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  QGB_CUDA_CHECK(cudaFuncSetAttribute(k_fft_yz_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  configured = smem;
-  return QGB_OK;
+  int rc;
+  if ((rc = raise_smem_limit(k_ifft_yz<T>, smem))) return rc;
+  if ((rc = raise_smem_limit(k_xpass<T>, smem))) return rc;
+  return raise_smem_limit(k_fft_yz_gather<T>, smem);
 }
 
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb,
@@ -717,21 +701,10 @@ template <typename T>
 static int launch_batched(const qgb_batch_item* items, const int* slab_item, const long long* slab_starts,
                           const int* row_item, const long long* row_starts, long long n_slab, long long n_row,
                           size_t smem_yz, size_t smem_x, cudaStream_t st) {
-  static size_t configured_yz = 0, configured_x = 0;
-  std::unique_lock<std::mutex> lock(g_attr_mu);
-  if (smem_yz > configured_yz) {
-    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_ifft_yz_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem_yz));
-    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_fft_yz_gather_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem_yz));
-    configured_yz = smem_yz;
-  }
-  if (smem_x > configured_x) {
-    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_xpass_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem_x));
-    configured_x = smem_x;
-  }
-  lock.unlock();
+  int rc;
+  if ((rc = raise_smem_limit(k_ifft_yz_batched<T>, smem_yz))) return rc;
+  if ((rc = raise_smem_limit(k_fft_yz_gather_batched<T>, smem_yz))) return rc;
+  if ((rc = raise_smem_limit(k_xpass_batched<T>, smem_x))) return rc;
   // Units per CTA: up to 8 while the grid keeps at least 32 CTAs per SM.
   auto upc_for = [](long long n) { return static_cast<int>(std::max(1LL, std::min(8LL, n / (152LL * 32)))); };
   auto ctas = [](long long n, int upc) { return static_cast<unsigned>((n + upc - 1) / upc); };
@@ -888,14 +861,7 @@ static int launch_density_chunk(const qgb_sphere& s, const LocalParams& lp, cons
   const int zs = density_zsplit(s, sizeof(T) == 8 ? QGB_F64 : QGB_F32);
   const int nz = (s.N[2] + zs - 1) / zs;
   const size_t smem = (static_cast<size_t>(s.N[0]) * (nz + 1) + s.N[0]) * sizeof(C2);
-  {
-    static size_t configured = 0;
-    std::lock_guard<std::mutex> lock(g_attr_mu);
-    if (smem > configured) {
-      QGB_CUDA_CHECK(cudaFuncSetAttribute(k_density_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      configured = smem;
-    }
-  }
+  if (int rc = raise_smem_limit(k_density_x<T>, smem)) return rc;
   // Groups of bands per CTA: enough CTAs to cover the SMs a few times over.
   const long long base = static_cast<long long>(s.N[1]) * zs * s.nk;
   const int groups = static_cast<int>(std::min<long long>(lp.nb, std::max<long long>(1, (4LL * 152 + base - 1) / base)));

@@ -8,6 +8,9 @@
 // qgb_apply_potential_static runs the same kernels as qgb_apply_potential with
 // its slab-plane scratch in a fixed file-scope device array instead of a
 // caller-provided buffer.  Nothing here allocates.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <mutex>
 
 #include "qgb_common.cuh"
@@ -26,22 +29,53 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 static constexpr int kMaxDevices = 64;
 static std::mutex g_scratch_mu;
 static void* g_scratch_addr[kMaxDevices];
+static unsigned long long g_scratch_ctx[kMaxDevices];  // context id the address belongs to
+
+// Unique id of the calling thread's current context (0 if the driver cannot
+// tell).  A device reset (cudaDeviceReset, or the primary context released)
+// reloads this module at a new address under a new context id.
+static unsigned long long current_context_id() {
+  static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
 
 // Device address of the scratch array on the current device.  The host-side
-// symbol is only a stand-in, so the address is looked up once per device with
-// that device current, and cached.
+// symbol is only a stand-in, so the address is looked up once per device (and
+// again after a device reset gave the device a new context) with that device
+// current, and cached.
 static int static_scratch(void** addr) {
   int dev = 0;
   QGB_CUDA_CHECK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(QGB_ERR_UNSUPPORTED, "device ordinal %d >= %d", dev, kMaxDevices);
+  // A thread that has not used the runtime yet may have no current context
+  // (id 0): that is no sign of a reset, so it keeps the cached address.
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (g_scratch_addr[dev] == nullptr) {
+  if (g_scratch_addr[dev] == nullptr || (ctx != 0 && g_scratch_ctx[dev] != ctx)) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess || p == nullptr)
       return fail(QGB_ERR_CUDA, "cudaGetSymbolAddress(static scratch) on device %d failed: %s", dev,
                   cudaGetErrorString(e));
     g_scratch_addr[dev] = p;
+    g_scratch_ctx[dev] = current_context_id();  // the lookup made the device's context current
   }
   *addr = g_scratch_addr[dev];
   return QGB_OK;

@@ -62,6 +62,17 @@ int fail(int code, const char* fmt, ...);
                          cudaGetErrorString(e_));                                   \
   } while (0)
 
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`.  The attribute belongs to the device's context, so the size
+// raised so far is kept per (kernel, device); the check and the raise are one
+// step under a lock, so host threads launching for different sizes cannot
+// lower a limit another thread is about to launch with.
+int raise_smem_limit(const void* kernel, size_t bytes);
+template <typename K>
+inline int raise_smem_limit(K* kernel, size_t bytes) {
+  return raise_smem_limit(reinterpret_cast<const void*>(kernel), bytes);
+}
+
 inline size_t elem_bytes(int dtype) { return dtype == QGB_F64 ? 16 : 8; }
 inline size_t real_bytes(int dtype) { return dtype == QGB_F64 ? 8 : 4; }
 

@@ -34,7 +34,8 @@ namespace tc {
 constexpr int BM = 128;            // MMA M (rows of A per CTA)
 constexpr int BK = 64;             // bf16 elements per stage along K (one 128 B swizzle atom)
 constexpr int kThreads = 128;
-constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s per pipeline wait
+constexpr unsigned long long kDrainNs = 2000000000ull;    // 2 s per drain wait
 
 enum Epi { EPI_PARTIAL = 0, EPI_ADD_HC = 1 };
 
@@ -49,6 +50,8 @@ struct GemmArgs {
   long long hc_batch_stride;
   int hc_ld, nb;
   int* err;                // device error word (0 = ok)
+  unsigned long long timeout_ns;  // limit of each pipeline wait (kTimeoutNs)
+  int skip_loads;          // test aid: the producer issues no copies, so the MMA wait runs out
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -75,18 +78,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase with the given parity; false on timeout or when
-// another thread already flagged an error.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+// Bounded wait for the phase with the given parity; false on timeout (error
+// `code` recorded) or when another thread already flagged an error.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code,
+                                          unsigned long long limit_ns) {
   const unsigned long long t0 = now_ns();
   for (unsigned it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 255u) {
       if (*reinterpret_cast<volatile int*>(err) != 0) return false;
-      if (now_ns() - t0 > kTimeoutNs) {
+      if (now_ns() - t0 > limit_ns) {
         atomicCAS(err, 0, code);
         return false;
       }
+    }
+  }
+}
+// Drain wait: for work this CTA has already issued (TMA copies into its
+// shared memory, MMAs into its TMEM), which must land before the CTA frees
+// TMEM or exits.  It ignores the error word (an error elsewhere does not
+// cancel issued work) and gives up only after its own limit.
+__device__ __forceinline__ bool mbar_drain(uint64_t* bar, uint32_t parity, int* err, int code) {
+  const unsigned long long t0 = now_ns();
+  for (unsigned it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u && now_ns() - t0 > kDrainNs) {
+      atomicCAS(err, 0, code);
+      return false;
     }
   }
 }
@@ -212,12 +230,12 @@ __global__ void __launch_bounds__(kThreads)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (threadIdx.x == 0 && niter > 0) {
+  if (threadIdx.x == 0 && niter > 0 && !args.skip_loads) {
     // ---------------- TMA producer ----------------
     int issued = 0;
     for (int it = 0; it < niter; ++it) {
       const int s = it % STAGES, use = it / STAGES;
-      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, args.err, 1)) break;
+      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, args.err, 1, args.timeout_ns)) break;
       const int seg = it / nkb, kb = kb0 + it % nkb;
       unsigned char* a_dst = smem + s * L::STAGE_BYTES;
       unsigned char* b_dst = a_dst + L::A_BYTES;
@@ -226,15 +244,18 @@ __global__ void __launch_bounds__(kThreads)
       tma_load_3d(b_dst, seg == 1 ? &mB_lo : &mB_hi, &full[s], kb * BK, n_tile * BN, batch);
       ++issued;
     }
-    // Drain: the last min(STAGES, issued) loads must have landed before exit.
+    // Drain: every load issued lands before exit.  Loads before the last
+    // STAGES were waited for through the empty barriers (their MMAs consumed
+    // them); the last min(STAGES, issued) are waited for here, even after an
+    // error.
     for (int it = max(0, issued - STAGES); it < issued; ++it)
-      mbar_wait(&full[it % STAGES], (it / STAGES) & 1, args.err, 2);
+      mbar_drain(&full[it % STAGES], (it / STAGES) & 1, args.err, 2);
   } else if (threadIdx.x == 32 && niter > 0) {
     // ---------------- MMA issuer ----------------
     constexpr uint32_t idesc = idesc_bf16_f32(BM, BN);
     for (int it = 0; it < niter; ++it) {
       const int s = it % STAGES, use = it / STAGES;
-      if (!mbar_wait(&full[s], use & 1, args.err, 3)) break;
+      if (!mbar_wait(&full[s], use & 1, args.err, 3, args.timeout_ns)) break;
       tc_fence_after();
       const uint32_t a_addr = smem_u32(smem + s * L::STAGE_BYTES);
       const uint32_t b_addr = a_addr + L::A_BYTES;
@@ -249,8 +270,11 @@ __global__ void __launch_bounds__(kThreads)
   __syncwarp();
 
   // ---------------- Epilogue: all four warps ----------------
+  // tmem_full is committed after every MMA the issuer launched (also when it
+  // stopped early), so this wait drains the tensor cores before TMEM is read
+  // or freed, error or not.
   bool ok = niter > 0;
-  if (ok) ok = mbar_wait(tmem_full, 0, args.err, 4);
+  if (ok) ok = mbar_drain(tmem_full, 0, args.err, 4);
   tc_fence_after();
   // tcgen05.ld is warp-collective: decide per warp.
   ok = __all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(args.err) == 0);
@@ -354,21 +378,18 @@ struct Operand {
 };
 
 template <int BN, int STAGES, int EPI>
-static int launch(const Operand& A, const Operand& B, int K, int batch, const GemmArgs& base_args,
+static int launch(const Operand& A, const Operand& B, int K, int batch, const GemmArgs& args_in,
                   cudaStream_t st) {
   using L = Smem<BN, STAGES>;
+  GemmArgs base_args = args_in;
+  if (base_args.timeout_ns == 0) base_args.timeout_ns = kTimeoutNs;
   CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
   int rc;
   if ((rc = make_map(&ma_hi, A.hi, K, A.rows, batch, A.ld, A.batch_stride, BM))) return rc;
   if ((rc = make_map(&ma_lo, A.lo, K, A.rows, batch, A.ld, A.batch_stride, BM))) return rc;
   if ((rc = make_map(&mb_hi, B.hi, K, B.rows, batch, B.ld, B.batch_stride, BN))) return rc;
   if ((rc = make_map(&mb_lo, B.lo, K, B.rows, batch, B.ld, B.batch_stride, BN))) return rc;
-  static bool configured = false;
-  if (!configured) {
-    QGB_CUDA_CHECK(cudaFuncSetAttribute(k_tc_gemm<BN, STAGES, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        L::TOTAL));
-    configured = true;
-  }
+  if ((rc = raise_smem_limit(k_tc_gemm<BN, STAGES, EPI>, L::TOTAL))) return rc;
   const int m_tiles = static_cast<int>((A.rows + BM - 1) / BM);
   const int n_tiles = static_cast<int>((B.rows + BN - 1) / BN);
   dim3 grid(m_tiles, n_tiles, batch * base_args.splits);
@@ -685,6 +706,31 @@ int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, con
 int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
                 int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, cudaStream_t st) {
   return nonlocal_tc_phase(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, ws, ws_bytes, err, 3, st);
+}
+
+// Test aid for the bounded waits: one CTA of the GEMM whose producer issues
+// no copies, so the MMA issuer's first wait runs out after `timeout_ns` and
+// records error 3; no copy or MMA is in flight when it returns.  Operands
+// are valid (M = 128, N = 64, K = 64 bf16 rows of `ab`, 128 + 64 rows of 64
+// elements), `ws` >= 128 * 64 floats.
+int tc_wait_timeout_test(const void* ab, float* ws, int* err, unsigned long long timeout_ns, cudaStream_t st) {
+  if (!ab || !ws || !err || timeout_ns == 0) return fail(QGB_ERR_INVALID, "tc_wait_timeout_test arguments");
+  const auto* a = static_cast<const __nv_bfloat16*>(ab);
+  const auto* b = a + 128 * 64;
+  GemmArgs g{};
+  g.M = 128;
+  g.N = 64;
+  g.K = 64;
+  g.kb_per_split = 1;
+  g.splits = 1;
+  g.partial = ws;
+  g.part_ld = 64;
+  g.part_rows = 128;
+  g.err = err;
+  g.timeout_ns = timeout_ns;
+  g.skip_loads = 1;
+  return launch<64, 4, EPI_PARTIAL>(Operand{a, a, 128, 64, 128 * 64}, Operand{b, b, 64, 64, 64 * 64}, 64, 1, g,
+                                    st);
 }
 
 // Plain TN GEMM for tests: D (FP32 [M][N]) = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T.

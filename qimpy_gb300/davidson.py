@@ -24,6 +24,7 @@ from typing import Optional
 import numpy as np
 import torch
 
+from . import ops
 from .electrons import Electrons, Wavefunction
 from .linalg import eigh, eighg
 
@@ -103,11 +104,12 @@ class Davidson:
         self._i_iter = 0
 
     def precondition(self, Cerr: Wavefunction, KEref: torch.Tensor) -> Wavefunction:
-        """Cerr / (x + exp(-x)), x = KE / KEref (qimpy/dft/electrons/_davidson.py:92-99)."""
-        ke = self.electrons.basis.ke
-        x = ke[:, None, :] / KEref[..., None]
-        x = x + torch.exp(-x)
-        return Wavefunction(Cerr.basis, coeff=Cerr.coeff / x.to(Cerr.coeff.real.dtype))
+        """Cerr / (x + exp(-x)), x = KE / KEref (qimpy/dft/electrons/_davidson.py:92-99),
+        one pass of qgb_residual (with zero eigenvalues, the residual of Cerr is Cerr)."""
+        out = torch.empty_like(Cerr.coeff)
+        zero = torch.zeros((Cerr.coeff.shape[0], Cerr.n_bands()), dtype=torch.float64, device=out.device)
+        ops.residual(Cerr.coeff, Cerr.coeff, zero, self.electrons.basis.ke, KEref, out=out)
+        return Wavefunction(Cerr.basis, coeff=out)
 
     def _regularize(self, C: Wavefunction, norm: torch.Tensor, i_iter: int) -> None:
         """Re-randomise null bands (qimpy/dft/electrons/_davidson.py:101-115) with
@@ -158,12 +160,16 @@ class Davidson:
         min_deig, i_best = np.inf, 0
         for self._i_iter in range(1, n_iterations + 1):
             n_bands_cur = el.C.n_bands()
-            eig_sel = el.eig[:, n_eigs_done:, None]
-            C_sel = el.C.bands(n_eigs_done) if n_eigs_done else el.C
-            HC_sel = HC.bands(n_eigs_done) if n_eigs_done else HC
-            KEref = C_sel.band_ke()
-            R = HC_sel - C_sel * eig_sel.to(C_sel.coeff.real.dtype)
-            Cexp = self.precondition(R, KEref)
+            basis = el.basis
+            # Expansion from the unconverged bands [n_eigs_done, n_bands_cur)
+            # (_davidson.py:177-183), in three band-wise passes: reference KE,
+            # preconditioned residual (with its norm), then null-band
+            # randomisation, normalisation and constrain; no host sync.
+            KEref = ops.band_norm_ke(el.C.coeff, basis.ke, b0=n_eigs_done, norm=False)[1]
+            Cexp = Wavefunction(basis, coeff=torch.empty((basis.nk, n_bands_cur - n_eigs_done, basis.n_tot),
+                                                         dtype=el.C.coeff.dtype, device=el.C.coeff.device))
+            norm_exp = ops.residual(HC.coeff, el.C.coeff, el.eig, basis.ke, KEref, b0=n_eigs_done, out=Cexp.coeff,
+                                    norm=not fp32)
             if fp32:
                 # Project span(C) out of the expansion (twice: classical
                 # Gram-Schmidt with re-orthogonalisation).  span(C, Cexp) and
@@ -171,11 +177,10 @@ class Davidson:
                 # new directions are a small part of Cexp, and keeping the rest
                 # would leave the overlap too ill-conditioned for FP32.
                 for _ in range(2):
-                    Cexp = Cexp - el.C @ (el.C ^ Cexp).wait()
-            norm_exp = Cexp.band_norm()
-            self._regularize(Cexp, norm_exp, self._i_iter)
-            Cexp *= (1.0 / norm_exp)
-            Cexp.constrain()
+                    ops.matmul(el.C.coeff, -ops.dot(el.C.coeff, Cexp.coeff), out=Cexp.coeff, accumulate=True)
+                norm_exp = Cexp.band_norm()
+            ops.normalize_bands(Cexp.coeff, basis.n_device, norm_exp, self._norm_cut, self._i_iter, basis.n_max,
+                                basis.ke)
             n_bands_exp = Cexp.n_bands()
             n_bands_new = n_bands_cur + n_bands_exp
             Cnew = el.C.cat(Cexp)
@@ -214,7 +219,7 @@ class Davidson:
             el.C = Cnew @ V_new
             HC = HC @ Vcur
             HC += HCexp @ Vexp
-            el.eig = eig_new[..., :n_bands_next]
+            el.eig = eig_new[..., :n_bands_next].contiguous()
             el.deig_max = deig_max
             if el.deig_max < min_deig:
                 min_deig, i_best = el.deig_max, self._i_iter
@@ -225,7 +230,7 @@ class Davidson:
                 # iterations; test residuals against a fresh H C.
                 HC = yield el.C
                 hpsi_bands += el.C.n_bands() * el.basis.nk
-                res = (HC - el.C * el.eig[..., None].to(el.C.coeff.real.dtype)).band_norm()
+                res = ops.residual(HC.coeff, el.C.coeff, el.eig, norm=True)
                 res_max = float(res[:, :n_bands].max())
                 if res_max >= self.residual_threshold:
                     converged = False

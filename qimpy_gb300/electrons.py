@@ -72,6 +72,14 @@ class Basis:
     def nk(self) -> int:
         return int(self.k.shape[0])
 
+    @property
+    def n_device(self) -> torch.Tensor:
+        """Sphere sizes n per k as an int32 device tensor."""
+        nd = getattr(self, "_n_device", None)
+        if nd is None:
+            nd = self._n_device = torch.from_numpy(np.asarray(self.n, dtype=np.int32)).to(self.device)
+        return nd
+
     def get_ke(self) -> torch.Tensor:
         """0.5 |k+G|^2 per k and basis entry (qimpy/dft/electrons/_basis.py:256-270)."""
         return self.ke
@@ -171,9 +179,8 @@ class Wavefunction:
     # --- algebra --------------------------------------------------------------
     def dot(self, other: "Wavefunction") -> Waitless:
         """[k, b1, b2] = sum_g conj(self) other (qimpy/dft/electrons/_wavefunction_dot.py:18-107);
-        FP64 result for both precisions."""
-        r = torch.matmul(self.coeff.conj(), other.coeff.transpose(1, 2))
-        return Waitless(r.to(torch.complex128))
+        FP64 result for both precisions (qgb_dot)."""
+        return Waitless(ops.dot(self.coeff, other.coeff))
 
     __xor__ = dot
     dot_O = dot
@@ -182,21 +189,18 @@ class Wavefunction:
         return self  # norm-conserving: identity (_wavefunction_dot.py:127-134)
 
     def matmul(self, mat: torch.Tensor) -> "Wavefunction":
-        """C @ M along bands (qimpy/dft/electrons/_wavefunction_dot.py:137-191)."""
-        M = mat.to(self.coeff.dtype)
-        return Wavefunction(self.basis, coeff=torch.matmul(M.transpose(1, 2), self.coeff))
+        """C @ M along bands (qimpy/dft/electrons/_wavefunction_dot.py:137-191; qgb_matmul)."""
+        return Wavefunction(self.basis, coeff=ops.matmul(self.coeff, mat))
 
     __matmul__ = matmul
 
     def band_norm(self) -> torch.Tensor:
-        """sqrt(sum_g |c|^2), FP64 (qimpy/dft/electrons/_wavefunction.py:226-236)."""
-        c = torch.view_as_real(self.coeff).double()
-        return c.square().sum(dim=(-2, -1)).sqrt()
+        """sqrt(sum_g |c|^2), FP64 (qimpy/dft/electrons/_wavefunction.py:226-236; qgb_band_norm_ke)."""
+        return ops.band_norm_ke(self.coeff)[0]
 
     def band_ke(self) -> torch.Tensor:
-        """sum_g |c|^2 KE, FP64 (qimpy/dft/electrons/_wavefunction.py:238-247)."""
-        c2 = torch.view_as_real(self.coeff).double().square().sum(dim=-1)
-        return torch.einsum("kbg,kg->kb", c2, self.basis.ke)
+        """sum_g |c|^2 KE, FP64 (qimpy/dft/electrons/_wavefunction.py:238-247; qgb_band_norm_ke)."""
+        return ops.band_norm_ke(self.coeff, self.basis.ke, norm=False)[1]
 
     def constrain(self) -> None:
         """Zero padded coefficients (qimpy/dft/electrons/_wavefunction.py:264-275)."""

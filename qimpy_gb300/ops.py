@@ -27,6 +27,8 @@ def _qdtype(t: torch.Tensor) -> int:
 
 
 def _check_wf(sphere: DeviceSphere, C: torch.Tensor, name: str = "C") -> int:
+    if C.is_conj() or C.is_neg():
+        raise ValueError(f"{name} carries a lazy conjugate/negative bit; pass t.resolve_conj()")
     if not C.is_cuda:
         raise RuntimeError(f"{name} must be a CUDA tensor (no CPU path)")
     if C.dtype != sphere.cdtype:
@@ -96,10 +98,81 @@ def project(beta: torch.Tensor, C: torch.Tensor, projT: torch.Tensor | None = No
     nb = C.shape[1]
     if C.dtype != beta.dtype or C.shape[0] != nk or C.shape[2] != n_tot:
         raise ValueError("beta / C mismatch")
+    beta, C = _plain(beta), _plain(C)
     projT = torch.empty((nk, nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
-    _lib.check(_lib.lib().qgb_project(_qdtype(C), beta.data_ptr(), C.data_ptr(), projT.data_ptr(), nk, P, nb,
-                                      n_tot, _stream()), "project")
+    lib = _lib.lib()
+    ws = workspace(lib.qgb_project_workspace_bytes(_qdtype(C), nk, P, nb, n_tot), C.device)
+    _lib.check(lib.qgb_project(_qdtype(C), beta.data_ptr(), C.data_ptr(), projT.data_ptr(), nk, P, nb, n_tot,
+                               ws.data_ptr(), ws.numel(), _stream()), "project")
     return projT
+
+
+def _plain(t: torch.Tensor) -> torch.Tensor:
+    """`t` with torch's lazy conjugate / negative bits applied and a dense
+    row-major layout: a contiguous tensor can still carry a conjugate bit (the
+    conjugate transpose of a column-major matrix is one), and its data pointer
+    then holds the unconjugated values."""
+    return t.resolve_conj().resolve_neg().contiguous()
+
+
+def _check_block(X: torch.Tensor, name: str) -> None:
+    if X.is_conj() or X.is_neg():
+        raise ValueError(f"{name} carries a lazy conjugate/negative bit; pass t.resolve_conj()")
+    if not X.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor (no CPU path)")
+    if X.dim() != 3 or not X.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous (nk, nb, n_tot) tensor")
+    _qdtype(X)
+
+
+def dot(X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """out[k, i, j] = sum_g conj(X[k, i, g]) Y[k, j, g] as complex128 (both
+    precisions; FP32 inputs are summed in FP32 per basis range, the ranges in FP64)."""
+    _check_block(X, "X")
+    _check_block(Y, "Y")
+    if X.dtype != Y.dtype or X.shape[0] != Y.shape[0] or X.shape[2] != Y.shape[2] or X.device != Y.device:
+        raise ValueError(f"dot operands differ: {tuple(X.shape)} {X.dtype} vs {tuple(Y.shape)} {Y.dtype}")
+    nk, nx, n_tot = X.shape
+    ny = Y.shape[1]
+    if out is None:
+        out = torch.empty((nk, nx, ny), dtype=torch.complex128, device=X.device)
+    elif out.dtype != torch.complex128 or tuple(out.shape) != (nk, nx, ny) or not out.is_contiguous():
+        raise ValueError("out must be a contiguous complex128 (nk, nx, ny) tensor")
+    if nk == 0 or nx == 0 or ny == 0:
+        return out
+    lib = _lib.lib()
+    qd = _qdtype(X)
+    ws = workspace(lib.qgb_dot_workspace_bytes(qd, nk, nx, ny, n_tot), X.device)
+    _lib.check(lib.qgb_dot(qd, X.data_ptr(), nx, Y.data_ptr(), ny, nk, n_tot, out.data_ptr(), ws.data_ptr(),
+                           ws.numel(), _stream()), "dot")
+    return out
+
+
+def matmul(C: torch.Tensor, M: torch.Tensor, out: torch.Tensor | None = None, accumulate: bool = False) -> torch.Tensor:
+    """out[k, j, g] (+)= sum_i M[k, i, j] C[k, i, g]; M is cast to C's dtype."""
+    _check_block(C, "C")
+    nk, n_in, n_tot = C.shape
+    if M.dim() == 2:
+        M = M.expand(nk, *M.shape)
+    if M.dim() != 3 or M.shape[0] != nk or M.shape[1] != n_in:
+        raise ValueError(f"matrix shape {tuple(M.shape)} does not match C {tuple(C.shape)}")
+    n_out = M.shape[2]
+    Mc = _plain(M.to(device=C.device, dtype=C.dtype))
+    if out is None:
+        if accumulate:
+            raise ValueError("accumulate needs an output tensor")
+        out = torch.empty((nk, n_out, n_tot), dtype=C.dtype, device=C.device)
+    elif out.dtype != C.dtype or tuple(out.shape) != (nk, n_out, n_tot) or not out.is_contiguous():
+        raise ValueError("out must be a contiguous (nk, n_out, n_tot) tensor of C's dtype")
+    if nk == 0 or n_out == 0:
+        return out
+    if n_in == 0:
+        if not accumulate:
+            out.zero_()
+        return out
+    _lib.check(_lib.lib().qgb_matmul(_qdtype(C), C.data_ptr(), n_in, nk, n_tot, Mc.data_ptr(), n_out, out.data_ptr(),
+                                     _lib.QGB_ACCUMULATE if accumulate else 0, _stream()), "matmul")
+    return out
 
 
 def apply_nonlocal(beta: torch.Tensor, D_blocks: torch.Tensor, projT: torch.Tensor, out: torch.Tensor,
@@ -110,6 +183,7 @@ def apply_nonlocal(beta: torch.Tensor, D_blocks: torch.Tensor, projT: torch.Tens
     nb = projT.shape[1]
     if n_atoms * pa != P:
         raise ValueError("D blocks do not cover the projectors")
+    beta, D_blocks, projT = _plain(beta), _plain(D_blocks), _plain(projT)
     work = torch.empty_like(projT) if work is None else work
     _lib.check(_lib.lib().qgb_apply_nonlocal(_qdtype(out), beta.data_ptr(), D_blocks.data_ptr(), n_atoms, pa,
                                              projT.data_ptr(), out.data_ptr(), nk, nb, n_tot, work.data_ptr(),
@@ -215,3 +289,72 @@ def hamiltonian_mixed(sphere: DeviceSphere, C: torch.Tensor, split: torch.Tensor
                                                 dptr, n_atoms, pa, pptr, ws.data_ptr(), ws.numel(), err.data_ptr(),
                                                 _stream()), "hamiltonian_mixed")
     return out, projT
+
+
+# ---------------------------------------------------------------------------
+# Band-wise Davidson passes
+# ---------------------------------------------------------------------------
+
+
+def band_norm_ke(C: torch.Tensor, ke: torch.Tensor | None = None, b0: int = 0, nb: int | None = None,
+                 norm: bool = True):
+    """(||C_b||, sum_g |C_bg|^2 KE_g) of bands [b0, b0 + nb) as FP64 (nk, nb)
+    tensors in one pass; either is None when not asked for (norm=False / ke None)."""
+    _check_block(C, "C")
+    nk, nb_all, n_tot = C.shape
+    nb = nb_all - b0 if nb is None else nb
+    out_n = torch.empty((nk, nb), dtype=torch.float64, device=C.device) if norm else None
+    out_k = torch.empty((nk, nb), dtype=torch.float64, device=C.device) if ke is not None else None
+    if ke is not None and (ke.dtype != torch.float64 or tuple(ke.shape) != (nk, n_tot) or not ke.is_contiguous()):
+        raise ValueError("ke must be a contiguous float64 (nk, n_tot) tensor")
+    _lib.check(_lib.lib().qgb_band_norm_ke(_qdtype(C), C.data_ptr(), nb_all, b0, nb, nk, n_tot,
+                                           ke.data_ptr() if ke is not None else None,
+                                           out_n.data_ptr() if out_n is not None else None,
+                                           out_k.data_ptr() if out_k is not None else None, _stream()),
+               "band_norm_ke")
+    return out_n, out_k
+
+
+def residual(HC: torch.Tensor, C: torch.Tensor, eig: torch.Tensor, ke: torch.Tensor | None = None,
+             KEref: torch.Tensor | None = None, b0: int = 0, out: torch.Tensor | None = None, norm: bool = False):
+    """R = HC_b - eig_b C_b for bands b0.. of C / HC (eig FP64 (nk, >= nb_all)),
+    preconditioned by 1 / (x + exp(-x)), x = KE / KEref_b, when KEref is given;
+    stored into `out` (nk, nb, n_tot) if given, its FP64 norms returned if `norm`."""
+    _check_block(C, "C")
+    _check_block(HC, "HC")
+    if HC.shape != C.shape or HC.dtype != C.dtype:
+        raise ValueError("HC and C differ in shape or dtype")
+    nk, nb_all, n_tot = C.shape
+    nb = nb_all - b0
+    if eig.dtype != torch.float64 or eig.dim() != 2 or eig.shape[0] != nk or eig.stride(1) != 1:
+        raise ValueError("eig must be float64 (nk, n) with unit column stride")
+    if KEref is not None:
+        if ke is None:
+            raise ValueError("preconditioning needs ke")
+        KEref = _plain(KEref.to(torch.float64))
+    if out is not None:
+        if out.dtype != C.dtype or tuple(out.shape) != (nk, nb, n_tot) or not out.is_contiguous():
+            raise ValueError("out must be a contiguous (nk, nb, n_tot) tensor of C's dtype")
+    nrm = torch.empty((nk, nb), dtype=torch.float64, device=C.device) if norm else None
+    _lib.check(_lib.lib().qgb_residual(_qdtype(C), HC.data_ptr(), C.data_ptr(), nb_all, b0, nb, nk, n_tot,
+                                       eig.data_ptr(), eig.stride(0), ke.data_ptr() if ke is not None else None,
+                                       KEref.data_ptr() if KEref is not None else None,
+                                       out.data_ptr() if out is not None else None,
+                                       nrm.data_ptr() if nrm is not None else None, _stream()), "residual")
+    return nrm
+
+
+def normalize_bands(X: torch.Tensor, n_dev: torch.Tensor, norm: torch.Tensor, norm_cut: float, seed: int,
+                    n_max: int, ke: torch.Tensor) -> None:
+    """In place: bands of X with norm < norm_cut re-randomised (the reference's
+    seeded generator; their norm set to 1), the others divided by their norm;
+    padding zeroed.  n_dev: int32 (nk,) sphere sizes on the device."""
+    _check_block(X, "X")
+    nk, nb, n_tot = X.shape
+    if norm.dtype != torch.float64 or tuple(norm.shape) != (nk, nb) or not norm.is_contiguous():
+        raise ValueError("norm must be a contiguous float64 (nk, nb) tensor")
+    if n_dev.dtype != torch.int32 or n_dev.numel() != nk:
+        raise ValueError("n_dev must be int32 (nk,)")
+    _lib.check(_lib.lib().qgb_normalize_bands(_qdtype(X), X.data_ptr(), nb, nk, n_tot, n_dev.data_ptr(),
+                                              norm.data_ptr(), float(norm_cut), int(seed), int(n_max),
+                                              ke.data_ptr(), _stream()), "normalize_bands")

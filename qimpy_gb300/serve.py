@@ -355,8 +355,11 @@ class EigenServer:
                 why = why or f"FP64 refinement not converged in {ref.iterations} sweeps (deig_max {ref.deig_max:.2e})"
             el = el64
         HC = el.hamiltonian(el.C)
-        res = (HC - el.C * el.eig[..., None].to(el.C.coeff.real.dtype)).band_norm()
+        res = ops.residual(HC.coeff, el.C.coeff, el.eig.contiguous(), norm=True)
         req.residual = float(res[:, : req.n_bands].max())
+        if converged and self.residual_threshold is not None and not req.residual < self.residual_threshold:
+            converged = False
+            why = f"residual {req.residual:.2e} above the target {self.residual_threshold:.0e}"
         eig = el.eig[:, : req.n_bands].detach().cpu().numpy()
         if not np.all(np.isfinite(eig)):
             raise RuntimeError("non-finite eigenvalues")

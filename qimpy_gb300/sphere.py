@@ -74,6 +74,9 @@ class SphereTables:
     rows: np.ndarray
     max_slabs: int
     max_rows: int
+    #: axes with a validated codelet factorisation; the others carry the
+    #: placeholder (N, 1) and are not complex-transformable
+    fft_axes: tuple = (0, 1, 2)
 
 
 def build_tables(fft_index: np.ndarray, n: np.ndarray, shape, fac=None, fft_axes=(0, 1, 2)) -> SphereTables:
@@ -124,7 +127,7 @@ def build_tables(fft_index: np.ndarray, n: np.ndarray, shape, fac=None, fft_axes
         row_start[k, ns:] = off
     rows_arr = np.concatenate(rows).astype(np.int32) if rows else np.zeros(1, np.int32)
     return SphereTables(nk, n_tot, (N0, N1, N2), fac, n.astype(np.int32), n_slabs, slab_start, slab_i0,
-                        yz, row_start, rows_arr, max_slabs, max_rows)
+                        yz, row_start, rows_arr, max_slabs, max_rows, tuple(sorted(fft_axes)))
 
 
 class DeviceSphere:
@@ -134,6 +137,11 @@ class DeviceSphere:
     def __init__(self, tables: SphereTables, ke: np.ndarray, device, dtype: torch.dtype):
         if dtype not in (torch.complex128, torch.complex64):
             raise ValueError("dtype must be complex128 or complex64")
+        if tuple(tables.fft_axes) != (0, 1, 2):
+            # Half-width (real-wavefunction) tables: their z axis is not a
+            # complex FFT axis, and the complex kernels would transform it as one.
+            raise ValueError(f"sphere tables with fft_axes={tables.fft_axes} are not complex-transformable "
+                             "on every axis; the complex-wavefunction kernels need all three")
         self.tables = tables
         self.device = torch.device(device)
         self.cdtype = dtype

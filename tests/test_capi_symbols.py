@@ -20,8 +20,8 @@ def lib():
     return _lib.lib()
 
 
-def declared_symbols():
-    with open(os.path.join(ROOT, "include", "qimpy_gb300.h")) as f:
+def declared_symbols(header: str = "qimpy_gb300.h"):
+    with open(os.path.join(ROOT, "include", header)) as f:
         text = f.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(qgb_[a-z0-9_]+)\s*\(", text)))
@@ -37,8 +37,23 @@ def test_every_declared_symbol_is_exported(lib):
     assert set(names) <= set(_lib.EXPORTED) | {"qgb_debug_violation"}
 
 
+def test_aux_library_exports_its_header(lib):
+    """Measurement and test aids live in libqimpy_gb300_aux.so, not in the product ABI."""
+    from qimpy_gb300 import _lib
+
+    aux = _lib.aux()
+    names = declared_symbols("qimpy_gb300_aux.h")
+    assert set(names) == set(_lib.AUX_EXPORTED)
+    for name in names:
+        assert hasattr(aux, name), name
+        assert name not in declared_symbols()
+    # Errors of the aux library are reported through the main library's message.
+    assert aux.qgb_tc_wait_timeout_test(None, None, None, 0, None) == 1
+    assert b"timeout" in lib.qgb_last_error()
+
+
 def test_abi_version_and_error_text(lib):
-    assert lib.qgb_abi_version() == 1
+    assert lib.qgb_abi_version() == 2
     from qimpy_gb300 import _lib
 
     # An invalid call fails on the host before touching a device.
@@ -70,3 +85,21 @@ def test_host_helpers(lib):
     nbytes = lib.qgb_potential_workspace_bytes(ct.byref(s), 3, 0)
     assert nbytes == 3 * t.nk * t.max_slabs * t.shape[1] * t.shape[2] * 16
     assert lib.qgb_potential_workspace_bytes(ct.byref(s), 3, 1) * 2 == nbytes
+
+
+def test_band_product_host_checks(lib):
+    """Workspace sizing of the split-K products and argument checks that fail
+    on the host, before any launch."""
+    # Small products need no partial sums; long bases are split over CTAs.
+    assert lib.qgb_dot_workspace_bytes(0, 1, 8, 8, 64) == 0
+    big = lib.qgb_dot_workspace_bytes(0, 1, 176, 352, 37073)
+    assert big > 0 and big % (176 * 352 * 16) == 0
+    assert lib.qgb_dot_workspace_bytes(1, 1, 176, 352, 37073) * 2 == big
+    assert lib.qgb_project_workspace_bytes(0, 1, 256, 32, 37073) % (256 * 32 * 16) == 0
+    assert lib.qgb_dot_workspace_bytes(9, 1, 8, 8, 64) == 0
+    assert lib.qgb_dot(9, None, 1, None, 1, 1, 64, None, None, 0, None) == 1
+    assert lib.qgb_dot(0, None, 1, None, 1, 1, 0, None, None, 0, None) == 1
+    assert lib.qgb_matmul(0, None, 2, 1, 64, None, 2, None, 4, None) == 1  # unknown flag
+    assert b"flags" in lib.qgb_last_error()
+    # nothing to do: no launch, success
+    assert lib.qgb_matmul(0, None, 2, 1, 64, None, 0, None, 0, None) == 0

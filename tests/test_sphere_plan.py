@@ -235,3 +235,19 @@ def test_real_wavefunction_slab_plan_matches_oracle():
     oh.real_symmetrize(out, b.iG[0], p.grid_shape)
     want = oh.apply_potential_real(p.V_r, b.fft_index, b.n, b.iG, C)
     assert np.abs(out - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def test_device_sphere_refuses_half_width_tables():
+    """Half-width (real-wavefunction) tables leave the z axis unfactorised; the
+    complex kernels would transform it as a complex axis, so DeviceSphere
+    refuses them before touching a device."""
+    import pytest
+    import torch
+
+    p = wl.get("tiny_gamma")
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape, real=True)
+    N0, N1, N2 = p.grid_shape
+    t = sp.build_tables(b.fft_index, b.n, (N0, N1, N2 // 2 + 1), fft_axes=(0, 1))
+    assert t.fft_axes == (0, 1)
+    with pytest.raises(ValueError, match="fft_axes"):
+        sp.DeviceSphere(t, b.ke, "cpu", torch.complex128)

@@ -42,7 +42,7 @@ def test_tc_gemm_bf16x3_exact_split(M, N, K):
     D = torch.empty((M, N), dtype=torch.float32, device=DEV)
     err = torch.zeros(1, dtype=torch.int32, device=DEV)
     ws = torch.empty(((M + 127) // 128 * 128) * 64, dtype=torch.float32, device=DEV)
-    rc = _lib.lib().qgb_tc_gemm_bf16x3(a_hi.data_ptr(), a_lo.data_ptr(), b_hi.data_ptr(), b_lo.data_ptr(), M, N, K,
+    rc = _lib.aux().qgb_tc_gemm_bf16x3(a_hi.data_ptr(), a_lo.data_ptr(), b_hi.data_ptr(), b_lo.data_ptr(), M, N, K,
                                         lda, ldb, D.data_ptr(), err.data_ptr(), ws.data_ptr(), ws.numel() * 4,
                                         torch.cuda.current_stream().cuda_stream)
     _lib.check(rc, "tc_gemm")
@@ -76,3 +76,21 @@ def test_nonlocal_tc_matches_oracle(name, nb):
     assert np.abs(got_proj - proj_ref).max() / np.abs(proj_ref).max() < 2e-5
     got = HC.cpu().numpy()
     assert np.abs(got - nl_ref).max() / np.abs(nl_ref).max() < 2e-5
+
+
+def test_bounded_wait_times_out_cleanly():
+    """A pipeline wait that runs out: the test launch's producer issues no
+    copies, so the MMA issuer's first wait gives up after 1 ms and records
+    error 3; the kernel frees its tensor memory and returns (no copy or MMA in
+    flight), and the context stays usable: a normal GEMM afterwards is exact."""
+    err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    ops_ = torch.zeros((192, 64), dtype=torch.bfloat16, device=DEV)
+    ws = torch.empty((128, 64), dtype=torch.float32, device=DEV)
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.check(_lib.aux().qgb_tc_wait_timeout_test(ops_.data_ptr(), ws.data_ptr(), err.data_ptr(), 1_000_000, st),
+               "tc_wait_timeout_test")
+    torch.cuda.synchronize()
+    assert int(err.item()) == 3
+    err.zero_()
+    test_tc_gemm_bf16x3_exact_split(128, 64, 64)
+    assert int(err.item()) == 0
