@@ -15,6 +15,7 @@ from __future__ import annotations
 import ctypes as ct
 import math
 from dataclasses import dataclass, field
+from typing import Optional
 
 import numpy as np
 import torch
@@ -159,11 +160,11 @@ class Instance:
                           torch.randn((self.nk, self.nb, self.n_tot), generator=g, device=dev))
         return (C / (1 + ke[:, None, :]) * mask[:, None, :]).to(self.dtype).contiguous()
 
-    def electrons(self, n_bands: int):
+    def electrons(self, n_bands: int, n_bands_extra: Optional[int] = None):
         """Electrons (mirror API) of this instance for an eigensolve of the lowest
-        `n_bands` bands (n_bands_extra = max(1, ceil(0.1 n_bands)), the
-        reference's default, qimpy/dft/electrons/_fillings.py:236-243), sharing
-        this instance's device data; start vectors orthonormalised."""
+        `n_bands` bands, sharing this instance's device data; start vectors
+        orthonormalised.  n_bands_extra defaults to max(1, ceil(0.1 n_bands)),
+        the reference's default (qimpy/dft/electrons/_fillings.py:236-243)."""
         from . import electrons as E
 
         spec = self.spec
@@ -183,7 +184,7 @@ class Instance:
         ions = E.Ions.__new__(E.Ions)
         ions.basis, ions.beta, ions.D = basis, self.beta, self.D
         ions.n_projectors, ions.beta_split, ions.beta_version = int(self.beta.shape[1]), self.split, 0
-        extra = max(1, int(math.ceil(0.1 * n_bands)))
+        extra = max(1, int(math.ceil(0.1 * n_bands))) if n_bands_extra is None else int(n_bands_extra)
         el = E.Electrons.__new__(E.Electrons)
         el.basis, el.ions, el.V_r = basis, ions, self.V_r
         el.n_bands, el.n_bands_extra = n_bands, extra
