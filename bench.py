@@ -611,6 +611,59 @@ def run_eigensolve_si64(args, local):
     return out
 
 
+def run_real_hpsi(args, local):
+    """H.psi of real (Gamma-point) wavefunctions on the half basis of the
+    64-atom Si cell (96^3, n_half = 18,561 of the 37,073-point sphere,
+    P = 256), 160 bands in blocks of 32, FP64 and FP32, through
+    qgb_hamiltonian_real (two real bands per complex transform).  Same timing
+    rules as the headline: CUDA events per step, 512 MB L2 flush between steps."""
+    import torch
+
+    from qimpy_gb300 import ops, real_basis as rbm, workloads as wl
+
+    dev = torch.device(f"cuda:{local}")
+    p = wl.get("si64")
+    half, full = rbm.gamma_bases(p.Gbasis, p.ke_cutoff, p.grid_shape)
+    beta_np = wl.make_projectors(p, half)
+    nb, block = p.n_bands, p.block_size or p.n_bands
+    C_np = wl.make_wavefunctions(p, half, nb)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    out = {"workload": f"si64 Gamma, real wavefunctions: n_half {int(half.n[0])}, {nb} bands in blocks of {block}"}
+    for form, cdt in (("fp64", torch.complex128), ("mixed", torch.complex64)):
+        rb = rbm.DeviceRealBasis(half, full, dev, cdt)
+        rb.set_potential(torch.from_numpy(p.V_r))
+        C = torch.from_numpy(C_np).to(dev, cdt)
+        beta = torch.from_numpy(beta_np).to(dev, cdt)
+        D = torch.from_numpy(p.D_atom).to(dev, cdt)
+        blocks = [C[:, s:s + block].contiguous() for s in range(0, nb, block)]
+        outs = [torch.empty_like(c) for c in blocks]
+        projT = torch.empty((1, block, beta.shape[1]), dtype=cdt, device=dev)
+        ws = ops.workspace(rb.workspace_bytes(block, beta.shape[1]), dev)
+
+        def step():
+            for c, o in zip(blocks, outs):
+                ops.hamiltonian_real(rb, c, beta, D, out=o, projT=projT[:, : c.shape[1]], ws=ws)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        t = float(np.sum(times))
+        out[form] = {"value": nb * args.steps / t, "unit": UNIT, "ms_per_step": 1e3 * t / args.steps}
+        del rb, C, beta, blocks, outs, ws
+        torch.cuda.empty_cache()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def run_batch(args, local):
     """Batched uneven instances: `args.batch` independent problems (cubic sides
     10/14/18/22 bohr, 2-16 atoms, Ecut 15-25 Ha, 8-64 bands, 1-8 k-points),
@@ -786,6 +839,10 @@ def main():
         "gpu_launches": mixed["launches_per_step"] * args.steps,
         "clocks": mixed["clocks"],
     }
+    real = run_real_hpsi(args, local)
+    real["over_complex_form"] = {"fp64": real["fp64"]["value"] / f64["value"],
+                                 "mixed": real["mixed"]["value"] / mixed["value"]}
+    out["real_wavefunctions_si64"] = real
     if not args.no_eigensolve:
         out["eigensolve_si2"] = run_eigensolves(args, local)
         out["eigensolve_si64"] = run_eigensolve_si64(args, local)

@@ -225,6 +225,14 @@ int qgb_project(int dtype, const void* beta, const void* C, void* projT, int nk,
 size_t qgb_dot_workspace_bytes(int dtype, int nk, int nx, int ny, int n_tot);
 int qgb_dot(int dtype, const void* X, int nx, const void* Y, int ny, int nk, int n_tot, void* out,
             void* workspace, size_t workspace_bytes, void* stream);
+/*
+ * The overlap of real (Gamma-point) wavefunctions on the half basis:
+ * out[i][j] = Re sum_g w_g conj(X[i][g]) Y[j][g] (imaginary part 0), weight
+ * FP64 [n_tot], workspace of qgb_dot_workspace_bytes with nk = 1 (the
+ * real-basis branch of qimpy/dft/electrons/_wavefunction_dot.py:55-88).
+ */
+int qgb_dot_real(int dtype, const void* X, int nx, const void* Y, int ny, int n_tot, const double* weight,
+                 void* out, void* workspace, size_t workspace_bytes, void* stream);
 
 /*
  * Band rotation out[k][j][g] = sum_i M[k][i][j] C[k][i][g] (+= with
@@ -264,12 +272,14 @@ size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int d
  * [b0, b0 + nb); ke FP64 [nk][n_tot]; per-band results FP64 [nk][nb]):
  *
  * qgb_band_norm_ke: norm = ||C_b||, band_ke = sum_g |C_bg|^2 KE_g (either may be
- *   NULL; ke may be NULL without band_ke).  Replaces Wavefunction.band_norm and
- *   band_ke (qimpy/dft/electrons/_wavefunction.py:226-247).
+ *   NULL; ke may be NULL without band_ke); with `weight` (FP64 [n_tot], may be
+ *   NULL) every |C_bg|^2 is weighted by w_g (real wavefunctions: 1 on the
+ *   Gz = 0 plane, 2 elsewhere).  Replaces Wavefunction.band_norm and band_ke
+ *   (qimpy/dft/electrons/_wavefunction.py:226-247).
  * qgb_residual: R = HC_b - eig[k][b0 + b] C_b (eig FP64 [nk][eig_ld]); with
  *   KEref (FP64 [nk][nb]) preconditioned as R / (x + exp(-x)), x = KE / KEref_b;
  *   stored to out [nk][nb][n_tot] (may be NULL) and reduced to norm (may be
- *   NULL).  Replaces the residual and Davidson.precondition
+ *   NULL, weighted like qgb_band_norm_ke).  Replaces the residual and Davidson.precondition
  *   (qimpy/dft/electrons/_davidson.py:92-99, 177-180).
  * qgb_normalize_bands: X [nk][nb][n_tot] in place: bands with norm < norm_cut
  *   are re-randomised with the reference's seeded generator (state (1 + seed)
@@ -281,12 +291,62 @@ size_t qgb_hamiltonian_workspace_bytes(const qgb_sphere* s, int nb, int P, int d
  *   _wavefunction_init.py:127-188; _wavefunction.py:264-275).  n: int32 [nk].
  */
 int qgb_band_norm_ke(int dtype, const void* C, int nb_all, int b0, int nb, int nk, int n_tot, const double* ke,
-                     double* norm, double* band_ke, void* stream);
+                     const double* weight, double* norm, double* band_ke, void* stream);
 int qgb_residual(int dtype, const void* HC, const void* C, int nb_all, int b0, int nb, int nk, int n_tot,
-                 const double* eig, int eig_ld, const double* ke, const double* KEref, void* out, double* norm,
-                 void* stream);
+                 const double* eig, int eig_ld, const double* ke, const double* KEref, const double* weight,
+                 void* out, double* norm, void* stream);
 int qgb_normalize_bands(int dtype, void* X, int nb, int nk, int n_tot, const int32_t* n, double* norm,
                         double norm_cut, long long seed, long long n_max, const double* ke, void* stream);
+
+/*
+ * Real (Gamma-point) wavefunctions: coefficients on the half-sphere basis
+ * Gz >= 0 of the reference's real-wavefunction mode
+ * (qimpy/dft/electrons/_basis_real.py:10-106; H-mesh basis, _basis.py:168),
+ * rows [nb][n_tot_half], with c(-G) = conj(c(G)) implied.  The local potential
+ * runs on the full Gamma sphere (a qgb_sphere with nk = 1 and the potential
+ * installed) with two real bands per complex transform.
+ *   pack[n_full][2]      per full-sphere entry G: (half index of G, -1) for
+ *                        Gz > 0; (half index of -G | bit 31 (conjugate), -1)
+ *                        for Gz < 0; (half index of G, half index of -G) on
+ *                        the Gz = 0 plane, whose Hermitian part is used
+ *   unpack[n_half][2]    full-sphere index of G and of -G of every half entry
+ *   plane[n_plane][2]    half index of each Gz = 0 entry and of its -G partner
+ *   ke[n_tot_half]       0.5 |G|^2, real of the call's dtype
+ *   weight[n_tot_half]   FP64 overlap weight: 1 on Gz = 0, 2 elsewhere, 0 on padding
+ */
+typedef struct qgb_real_map {
+  int32_t n_half, n_tot_half;  /* half-basis entries, padded row length */
+  int32_t n_full, n_tot_full;  /* full-sphere entries, its padded row length (the sphere's n_tot) */
+  int32_t n_plane;             /* half entries with Gz = 0 */
+  const int32_t* pack;
+  const int32_t* unpack;
+  const int32_t* plane;
+  const void* ke;
+  const double* weight;
+} qgb_real_map;
+
+/*
+ * HC = KE C + V C + beta D <beta|C> for real wavefunctions (replaces
+ * Electrons.hamiltonian, qimpy/dft/electrons/_hamiltonian.py:7-29, in the
+ * reference's real-wavefunction mode): the local potential of ceil(nb / 2)
+ * packed full-sphere rows, then <beta|C> = Re sum_G w_G conj(beta) C (projT
+ * [nb][P], imaginary parts zero; _wavefunction_dot.py:55-88) and the
+ * back-projection.  C, HC [nb][n_tot_half] of `dtype` (must not alias);
+ * beta [P][n_tot_half]; D per-atom blocks [n_atoms][pa][pa].  The Gz = 0 plane
+ * of the local term is Hermitian.  Workspace of
+ * qgb_hamiltonian_real_workspace_bytes.
+ */
+size_t qgb_hamiltonian_real_workspace_bytes(const qgb_sphere* full, const qgb_real_map* map, int nb, int P,
+                                            int dtype);
+int qgb_hamiltonian_real(const qgb_sphere* full, const qgb_real_map* map, int dtype, const void* C, void* HC,
+                         int nb, const void* beta, const void* D, int n_atoms, int pa, void* projT, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
+/*
+ * X [nb][n_tot_half] in place: c(G) = (c(G) + conj(c(-G))) / 2 on the Gz = 0
+ * plane (replaces BasisReal.symmetrize, qimpy/dft/electrons/_basis_real.py:68-106).
+ */
+int qgb_symmetrize_real(int dtype, const qgb_real_map* map, void* X, int nb, void* stream);
 
 /*
  * Mixed-precision nonlocal term on the tcgen05 tensor cores (split-BF16x3,

@@ -34,6 +34,14 @@ class QgbSphere(ct.Structure):
     ]
 
 
+class QgbRealMap(ct.Structure):
+    """Mirror of ``struct qgb_real_map``."""
+
+    _fields_ = [("n_half", ct.c_int32), ("n_tot_half", ct.c_int32), ("n_full", ct.c_int32),
+                ("n_tot_full", ct.c_int32), ("n_plane", ct.c_int32), ("pack", ct.c_void_p), ("unpack", ct.c_void_p),
+                ("plane", ct.c_void_p), ("ke", ct.c_void_p), ("weight", ct.c_void_p)]
+
+
 class QgbBatchItem(ct.Structure):
     """Mirror of ``struct qgb_batch_item``."""
 
@@ -64,12 +72,20 @@ _SIGS = {
     "qgb_dot": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p,
                            ct.c_void_p, ct.c_size_t, ct.c_void_p]),
     "qgb_band_norm_ke": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
-                                    ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+                                    ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "qgb_residual": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
-                                ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                 ct.c_void_p]),
     "qgb_normalize_bands": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
                                        ct.c_double, ct.c_longlong, ct.c_longlong, ct.c_void_p, ct.c_void_p]),
+    "qgb_dot_real": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p,
+                                ct.c_void_p, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_hamiltonian_real_workspace_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.POINTER(QgbRealMap), ct.c_int,
+                                                           ct.c_int, ct.c_int]),
+    "qgb_hamiltonian_real": (ct.c_int, [ct.POINTER(QgbSphere), ct.POINTER(QgbRealMap), ct.c_int, ct.c_void_p,
+                                        ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
+                                        ct.c_void_p, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_symmetrize_real": (ct.c_int, [ct.c_int, ct.POINTER(QgbRealMap), ct.c_void_p, ct.c_int, ct.c_void_p]),
     "qgb_matmul": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int,
                               ct.c_void_p, ct.c_uint, ct.c_void_p]),
     "qgb_apply_nonlocal": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p,

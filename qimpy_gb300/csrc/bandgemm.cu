@@ -17,7 +17,7 @@
 #include <algorithm>
 #include <type_traits>
 
-#include "qgb_common.cuh"
+#include "bandgemm.cuh"
 
 namespace qgb {
 namespace bg {
@@ -64,6 +64,8 @@ struct GramArgs {
   void* out;                   // splits == 1: OutT at out + k*out_batch + i*oi + j*oj
   long long out_batch;
   int oi, oj;
+  const double* weight;        // optional per-g weight w_g (shared by all k): sum_g w_g conj(A) B
+  int real_out;                // keep only the real part (imaginary part written as 0)
 };
 
 template <typename T, typename OutT>
@@ -90,7 +92,13 @@ __global__ void __launch_bounds__(256) k_gram(const GramArgs a) {
       const int e = tid + 256 * r, row = e >> 4, gg = e & 15, g = g0 + gg;
       const bool g_ok = g < g_end;
       As[gg][row] = (g_ok && i0 + row < a.M) ? A[static_cast<long long>(i0 + row) * a.lda + g] : mk<T>(T(0), T(0));
-      Bs[gg][row] = (g_ok && j0 + row < a.N) ? B[static_cast<long long>(j0 + row) * a.ldb + g] : mk<T>(T(0), T(0));
+      C2 bv = (g_ok && j0 + row < a.N) ? B[static_cast<long long>(j0 + row) * a.ldb + g] : mk<T>(T(0), T(0));
+      if (a.weight != nullptr && g_ok) {
+        const T w = static_cast<T>(a.weight[g]);
+        bv.x *= w;
+        bv.y *= w;
+      }
+      Bs[gg][row] = bv;
     }
     __syncthreads();
 #pragma unroll
@@ -117,7 +125,7 @@ __global__ void __launch_bounds__(256) k_gram(const GramArgs a) {
         const int j = j0 + tx * 4 + q;
         if (i < a.M && j < a.N)
           out[static_cast<long long>(i) * a.oi + static_cast<long long>(j) * a.oj] =
-              mk<OutT>(static_cast<OutT>(acc[p][q].x), static_cast<OutT>(acc[p][q].y));
+              mk<OutT>(static_cast<OutT>(acc[p][q].x), a.real_out ? OutT(0) : static_cast<OutT>(acc[p][q].y));
       }
     }
   } else {
@@ -139,7 +147,7 @@ __global__ void __launch_bounds__(256) k_gram(const GramArgs a) {
 // or better), written with the caller's output strides.
 template <typename T, typename OutT>
 __global__ void k_gram_reduce(const cplx_t<T>* __restrict__ partial, int splits, int nk, int M, int N,
-                              cplx_t<OutT>* __restrict__ out, long long out_batch, int oi, int oj) {
+                              cplx_t<OutT>* __restrict__ out, long long out_batch, int oi, int oj, int real_out) {
   using Acc = typename std::conditional<sizeof(T) >= sizeof(OutT), T, OutT>::type;
   const long long per_k = static_cast<long long>(M) * N;
   const long long total = per_k * nk;
@@ -155,7 +163,7 @@ __global__ void k_gram_reduce(const cplx_t<T>* __restrict__ partial, int splits,
       im += static_cast<Acc>(v.y);
     }
     out[k * out_batch + static_cast<long long>(i) * oi + static_cast<long long>(j) * oj] =
-        mk<OutT>(static_cast<OutT>(re), static_cast<OutT>(im));
+        mk<OutT>(static_cast<OutT>(re), real_out ? OutT(0) : static_cast<OutT>(im));
   }
 }
 
@@ -295,7 +303,7 @@ size_t gram_workspace_bytes(int dtype, int nk, int M, int N, int K) {
 // out(i, j) of type out_dtype (complex) = sum_g conj(A(i, g)) B(j, g), per k.
 int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, const void* B, long long b_batch,
          int ldb, int nk, int M, int N, int K, void* out, long long out_batch, int oi, int oj, void* ws,
-         size_t ws_bytes, cudaStream_t st) {
+         size_t ws_bytes, cudaStream_t st, const double* weight, bool real_out) {
   if (nk < 0 || M < 0 || N < 0 || K < 0) return fail(QGB_ERR_INVALID, "negative gram extent");
   if (nk == 0 || M == 0 || N == 0) return QGB_OK;
   if (!A || !B || !out) return fail(QGB_ERR_INVALID, "NULL pointer in gram");
@@ -306,7 +314,8 @@ int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, co
   const GramPlan p = gram_plan(nk, M, N, K, elem_bytes(dtype));
   if (p.splits > 1 && (!ws || ws_bytes < p.partial_bytes))
     return fail(QGB_ERR_WORKSPACE, "gram workspace %zu B < %zu B", ws_bytes, p.partial_bytes);
-  GramArgs g{A, B, a_batch, b_batch, lda, ldb, M, N, K, p.splits, p.g_per_split, ws, out, out_batch, oi, oj};
+  GramArgs g{A, B, a_batch, b_batch, lda, ldb, M, N, K, p.splits, p.g_per_split, ws, out, out_batch, oi, oj,
+             weight, real_out ? 1 : 0};
   const dim3 grid(p.ti, p.tj, nk * p.splits);
   if (dtype == QGB_F64) {
     k_gram<double, double><<<grid, 256, 0, st>>>(g);
@@ -321,13 +330,13 @@ int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, co
     const unsigned blocks = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 8 * kSms));
     if (dtype == QGB_F64) {
       k_gram_reduce<double, double><<<blocks, 256, 0, st>>>(static_cast<const double2*>(ws), p.splits, nk, M, N,
-                                                            static_cast<double2*>(out), out_batch, oi, oj);
+                                                            static_cast<double2*>(out), out_batch, oi, oj, g.real_out);
     } else if (out_dtype == QGB_F64) {
       k_gram_reduce<float, double><<<blocks, 256, 0, st>>>(static_cast<const float2*>(ws), p.splits, nk, M, N,
-                                                           static_cast<double2*>(out), out_batch, oi, oj);
+                                                           static_cast<double2*>(out), out_batch, oi, oj, g.real_out);
     } else {
       k_gram_reduce<float, float><<<blocks, 256, 0, st>>>(static_cast<const float2*>(ws), p.splits, nk, M, N,
-                                                          static_cast<float2*>(out), out_batch, oi, oj);
+                                                          static_cast<float2*>(out), out_batch, oi, oj, g.real_out);
     }
     QGB_LAUNCH_CHECK("k_gram_reduce");
   }

@@ -7,7 +7,7 @@
 #include <unordered_map>
 #include <utility>
 
-#include "qgb_common.cuh"
+#include "bandgemm.cuh"
 
 namespace qgb {
 
@@ -53,13 +53,6 @@ int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, c
 size_t project_workspace_bytes(int dtype, int nk, int P, int nb, int n_tot);
 int project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb, int n_tot, void* ws,
             size_t ws_bytes, cudaStream_t st);
-size_t gram_workspace_bytes(int dtype, int nk, int M, int N, int K);
-int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, const void* B, long long b_batch,
-         int ldb, int nk, int M, int N, int K, void* out, long long out_batch, int oi, int oj, void* ws,
-         size_t ws_bytes, cudaStream_t st);
-int rotate(int dtype, const void* X, long long x_batch, int ldx, const void* W, long long w_batch, int wi, int wj,
-           int nk, int Kin, int Nout, int G, void* out, long long out_batch, int ldo, bool accumulate,
-           cudaStream_t st);
 int apply_nonlocal(int dtype, const void* beta, const void* D, int n_atoms, int pa, const void* projT,
                    void* out, int nk, int nb, int n_tot, void* work, cudaStream_t st);
 #ifdef QGB_DEBUG_CHECKS
@@ -182,6 +175,16 @@ int qgb_dot(int dtype, const void* X, int nx, const void* Y, int ny, int nk, int
   return gram(dtype, QGB_F64, X, static_cast<long long>(nx) * n_tot, n_tot, Y, static_cast<long long>(ny) * n_tot,
               n_tot, nk, nx, ny, n_tot, out, static_cast<long long>(nx) * ny, ny, 1, workspace, workspace_bytes,
               static_cast<cudaStream_t>(stream));
+}
+
+int qgb_dot_real(int dtype, const void* X, int nx, const void* Y, int ny, int n_tot, const double* weight, void* out,
+                 void* workspace, size_t workspace_bytes, void* stream) {
+  if (dtype != QGB_F64 && dtype != QGB_F32) return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
+  if (nx < 0 || ny < 0 || n_tot < 1) return fail(QGB_ERR_INVALID, "bad dot sizes");
+  if (!weight) return fail(QGB_ERR_INVALID, "NULL weight");
+  return gram(dtype, QGB_F64, X, static_cast<long long>(nx) * n_tot, n_tot, Y, static_cast<long long>(ny) * n_tot,
+              n_tot, 1, nx, ny, n_tot, out, static_cast<long long>(nx) * ny, ny, 1, workspace, workspace_bytes,
+              static_cast<cudaStream_t>(stream), weight, true);
 }
 
 int qgb_matmul(int dtype, const void* C, int n_in, int nk, int n_tot, const void* M, int n_out, void* out,

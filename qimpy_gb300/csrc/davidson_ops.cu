@@ -36,7 +36,8 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_band_stats(const cplx_t<T>* __restrict__ C, int nb_all, int b0, int nb, int n_tot,
-                 const double* __restrict__ ke, double* __restrict__ norm, double* __restrict__ bke) {
+                 const double* __restrict__ ke, const double* __restrict__ weight, double* __restrict__ norm,
+                 double* __restrict__ bke) {
   __shared__ double red[2][kThreads / 32];
   const int row = blockIdx.x, k = row / nb, b = row - k * nb;
   const cplx_t<T>* c = C + (static_cast<long long>(k) * nb_all + b0 + b) * n_tot;
@@ -44,7 +45,8 @@ __global__ void __launch_bounds__(kThreads)
   double s0 = 0.0, s1 = 0.0;
   for (int g = threadIdx.x; g < n_tot; g += kThreads) {
     const cplx_t<T> v = c[g];
-    const double a = static_cast<double>(v.x) * v.x + static_cast<double>(v.y) * v.y;
+    double a = static_cast<double>(v.x) * v.x + static_cast<double>(v.y) * v.y;
+    if (weight) a *= weight[g];
     s0 += a;
     if (kek) s1 += a * kek[g];
   }
@@ -60,7 +62,8 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_residual(const cplx_t<T>* __restrict__ HC, const cplx_t<T>* __restrict__ C, int nb_all, int b0, int nb,
                int n_tot, const double* __restrict__ eig, int eig_ld, const double* __restrict__ ke,
-               const double* __restrict__ KEref, cplx_t<T>* __restrict__ out, double* __restrict__ norm) {
+               const double* __restrict__ KEref, const double* __restrict__ weight, cplx_t<T>* __restrict__ out,
+               double* __restrict__ norm) {
   __shared__ double red[kThreads / 32];
   const int row = blockIdx.x, k = row / nb, b = row - k * nb;
   const long long off = (static_cast<long long>(k) * nb_all + b0 + b) * n_tot;
@@ -82,7 +85,8 @@ __global__ void __launch_bounds__(kThreads)
       ry /= x;
     }
     if (o) o[g] = mk<T>(rx, ry);
-    s += static_cast<double>(rx) * rx + static_cast<double>(ry) * ry;
+    const double a = static_cast<double>(rx) * rx + static_cast<double>(ry) * ry;
+    s += weight ? a * weight[g] : a;
   }
   if (norm) {
     s = block_sum(s, red);
@@ -151,7 +155,7 @@ static int rows_ok(int nk, int nb, int n_tot) {
 using namespace qgb;
 
 extern "C" int qgb_band_norm_ke(int dtype, const void* C, int nb_all, int b0, int nb, int nk, int n_tot,
-                                const double* ke, double* norm, double* band_ke, void* stream) {
+                                const double* ke, const double* weight, double* norm, double* band_ke, void* stream) {
   if (int rc = rows_ok(nk, nb, n_tot)) return rc;
   if (b0 < 0 || b0 + nb > nb_all) return fail(QGB_ERR_INVALID, "bands [%d, %d) outside %d", b0, b0 + nb, nb_all);
   if (nk * nb == 0) return QGB_OK;
@@ -159,10 +163,10 @@ extern "C" int qgb_band_norm_ke(int dtype, const void* C, int nb_all, int b0, in
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (dtype == QGB_F64)
     k_band_stats<double><<<nk * nb, kThreads, 0, st>>>(static_cast<const double2*>(C), nb_all, b0, nb, n_tot, ke,
-                                                       norm, band_ke);
+                                                       weight, norm, band_ke);
   else if (dtype == QGB_F32)
-    k_band_stats<float><<<nk * nb, kThreads, 0, st>>>(static_cast<const float2*>(C), nb_all, b0, nb, n_tot, ke, norm,
-                                                      band_ke);
+    k_band_stats<float><<<nk * nb, kThreads, 0, st>>>(static_cast<const float2*>(C), nb_all, b0, nb, n_tot, ke,
+                                                      weight, norm, band_ke);
   else
     return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);
   QGB_LAUNCH_CHECK("k_band_stats");
@@ -170,8 +174,8 @@ extern "C" int qgb_band_norm_ke(int dtype, const void* C, int nb_all, int b0, in
 }
 
 extern "C" int qgb_residual(int dtype, const void* HC, const void* C, int nb_all, int b0, int nb, int nk, int n_tot,
-                            const double* eig, int eig_ld, const double* ke, const double* KEref, void* out,
-                            double* norm, void* stream) {
+                            const double* eig, int eig_ld, const double* ke, const double* KEref, const double* weight,
+                            void* out, double* norm, void* stream) {
   if (int rc = rows_ok(nk, nb, n_tot)) return rc;
   if (b0 < 0 || b0 + nb > nb_all || b0 + nb > eig_ld)
     return fail(QGB_ERR_INVALID, "bands [%d, %d) outside %d (eig_ld %d)", b0, b0 + nb, nb_all, eig_ld);
@@ -180,11 +184,11 @@ extern "C" int qgb_residual(int dtype, const void* HC, const void* C, int nb_all
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (dtype == QGB_F64)
     k_residual<double><<<nk * nb, kThreads, 0, st>>>(static_cast<const double2*>(HC), static_cast<const double2*>(C),
-                                                     nb_all, b0, nb, n_tot, eig, eig_ld, ke, KEref,
+                                                     nb_all, b0, nb, n_tot, eig, eig_ld, ke, KEref, weight,
                                                      static_cast<double2*>(out), norm);
   else if (dtype == QGB_F32)
     k_residual<float><<<nk * nb, kThreads, 0, st>>>(static_cast<const float2*>(HC), static_cast<const float2*>(C),
-                                                    nb_all, b0, nb, n_tot, eig, eig_ld, ke, KEref,
+                                                    nb_all, b0, nb, n_tot, eig, eig_ld, ke, KEref, weight,
                                                     static_cast<float2*>(out), norm);
   else
     return fail(QGB_ERR_INVALID, "unknown dtype %d", dtype);

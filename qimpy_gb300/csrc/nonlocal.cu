@@ -8,19 +8,9 @@
 //   out[k][b][g]  += sum_p beta[k][p][g] Dp[k][b][p]         (rotate, accumulate)
 // with the band-space product kernels of bandgemm.cu (hand-written, FP64 or
 // FP32; the mixed form's tensor-core chain is tc_gemm.cu).
-#include "qgb_common.cuh"
+#include "bandgemm.cuh"
 
 namespace qgb {
-
-size_t gram_workspace_bytes(int dtype, int nk, int M, int N, int K);
-int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, const void* B, long long b_batch,
-         int ldb, int nk, int M, int N, int K, void* out, long long out_batch, int oi, int oj, void* ws,
-         size_t ws_bytes, cudaStream_t st);
-int rotate(int dtype, const void* X, long long x_batch, int ldx, const void* W, long long w_batch, int wi, int wj,
-           int nk, int Kin, int Nout, int G, void* out, long long out_batch, int ldo, bool accumulate,
-           cudaStream_t st);
-int dapply(int dtype, const void* proj, const void* D, int n_atoms, int pa, int nb, int nk, void* Dp,
-           cudaStream_t st);
 
 size_t project_workspace_bytes(int dtype, int nk, int P, int nb, int n_tot) {
   return gram_workspace_bytes(dtype, nk, P, nb, n_tot);

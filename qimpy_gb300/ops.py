@@ -297,9 +297,10 @@ def hamiltonian_mixed(sphere: DeviceSphere, C: torch.Tensor, split: torch.Tensor
 
 
 def band_norm_ke(C: torch.Tensor, ke: torch.Tensor | None = None, b0: int = 0, nb: int | None = None,
-                 norm: bool = True):
+                 norm: bool = True, weight: torch.Tensor | None = None):
     """(||C_b||, sum_g |C_bg|^2 KE_g) of bands [b0, b0 + nb) as FP64 (nk, nb)
-    tensors in one pass; either is None when not asked for (norm=False / ke None)."""
+    tensors in one pass; either is None when not asked for (norm=False / ke None);
+    `weight` (FP64 (n_tot,)) weights every |C_bg|^2 (real wavefunctions)."""
     _check_block(C, "C")
     nk, nb_all, n_tot = C.shape
     nb = nb_all - b0 if nb is None else nb
@@ -309,14 +310,24 @@ def band_norm_ke(C: torch.Tensor, ke: torch.Tensor | None = None, b0: int = 0, n
         raise ValueError("ke must be a contiguous float64 (nk, n_tot) tensor")
     _lib.check(_lib.lib().qgb_band_norm_ke(_qdtype(C), C.data_ptr(), nb_all, b0, nb, nk, n_tot,
                                            ke.data_ptr() if ke is not None else None,
+                                           _weight_ptr(weight, n_tot),
                                            out_n.data_ptr() if out_n is not None else None,
                                            out_k.data_ptr() if out_k is not None else None, _stream()),
                "band_norm_ke")
     return out_n, out_k
 
 
+def _weight_ptr(weight: torch.Tensor | None, n_tot: int):
+    if weight is None:
+        return None
+    if weight.dtype != torch.float64 or weight.numel() != n_tot or not weight.is_contiguous() or not weight.is_cuda:
+        raise ValueError("weight must be a contiguous float64 CUDA tensor of n_tot entries")
+    return weight.data_ptr()
+
+
 def residual(HC: torch.Tensor, C: torch.Tensor, eig: torch.Tensor, ke: torch.Tensor | None = None,
-             KEref: torch.Tensor | None = None, b0: int = 0, out: torch.Tensor | None = None, norm: bool = False):
+             KEref: torch.Tensor | None = None, b0: int = 0, out: torch.Tensor | None = None, norm: bool = False,
+             weight: torch.Tensor | None = None):
     """R = HC_b - eig_b C_b for bands b0.. of C / HC (eig FP64 (nk, >= nb_all)),
     preconditioned by 1 / (x + exp(-x)), x = KE / KEref_b, when KEref is given;
     stored into `out` (nk, nb, n_tot) if given, its FP64 norms returned if `norm`."""
@@ -339,6 +350,7 @@ def residual(HC: torch.Tensor, C: torch.Tensor, eig: torch.Tensor, ke: torch.Ten
     _lib.check(_lib.lib().qgb_residual(_qdtype(C), HC.data_ptr(), C.data_ptr(), nb_all, b0, nb, nk, n_tot,
                                        eig.data_ptr(), eig.stride(0), ke.data_ptr() if ke is not None else None,
                                        KEref.data_ptr() if KEref is not None else None,
+                                       _weight_ptr(weight, n_tot),
                                        out.data_ptr() if out is not None else None,
                                        nrm.data_ptr() if nrm is not None else None, _stream()), "residual")
     return nrm
@@ -358,3 +370,71 @@ def normalize_bands(X: torch.Tensor, n_dev: torch.Tensor, norm: torch.Tensor, no
     _lib.check(_lib.lib().qgb_normalize_bands(_qdtype(X), X.data_ptr(), nb, nk, n_tot, n_dev.data_ptr(),
                                               norm.data_ptr(), float(norm_cut), int(seed), int(n_max),
                                               ke.data_ptr(), _stream()), "normalize_bands")
+
+
+# ---------------------------------------------------------------------------
+# Real (Gamma-point) wavefunctions on the half basis
+# ---------------------------------------------------------------------------
+
+
+def _check_real(rb, C: torch.Tensor, name: str = "C") -> int:
+    _check_block(C, name)
+    if C.dtype != rb.cdtype or C.shape[0] != 1 or C.shape[2] != rb.n_tot:
+        raise ValueError(f"{name} {tuple(C.shape)} {C.dtype} is not (1, nb, {rb.n_tot}) {rb.cdtype}")
+    return C.shape[1]
+
+
+def hamiltonian_real(rb, C: torch.Tensor, beta: torch.Tensor | None, D_blocks: torch.Tensor | None,
+                     out: torch.Tensor | None = None, projT: torch.Tensor | None = None,
+                     ws: torch.Tensor | None = None):
+    """(HC, projT) of real wavefunctions C (1, nb, n_tot_half) on the
+    ``DeviceRealBasis`` rb: HC = KE C + V C + beta D <beta|C> with the
+    weighted real projections (one C-ABI call)."""
+    nb = _check_real(rb, C)
+    out = torch.empty_like(C) if out is None else out
+    _check_real(rb, out, "out")
+    if beta is None or beta.shape[1] == 0:
+        n_atoms, pa, P = 0, 0, 0
+        bptr = dptr = pptr = 0
+    else:
+        _check_real(rb, beta, "beta")
+        n_atoms, pa, _ = D_blocks.shape
+        P = beta.shape[1]
+        if D_blocks.dtype != C.dtype or not D_blocks.is_contiguous() or n_atoms * pa != P:
+            raise ValueError("D_blocks must be contiguous (n_atoms, pa, pa) of C's dtype with n_atoms * pa = P")
+        projT = torch.empty((1, nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
+        bptr, dptr, pptr = beta.data_ptr(), D_blocks.data_ptr(), projT.data_ptr()
+    if ws is None:
+        ws = workspace(rb.workspace_bytes(nb, P), C.device)
+    _lib.check(_lib.lib().qgb_hamiltonian_real(ct.byref(rb.sphere.struct), ct.byref(rb.struct), rb.qdtype,
+                                               C.data_ptr(), out.data_ptr(), nb, bptr, dptr, n_atoms, pa, pptr,
+                                               ws.data_ptr(), ws.numel(), _stream()), "hamiltonian_real")
+    return out, projT
+
+
+def dot_real(X: torch.Tensor, Y: torch.Tensor, weight: torch.Tensor, out: torch.Tensor | None = None):
+    """out[0, i, j] = Re sum_g w_g conj(X[0, i, g]) Y[0, j, g] as complex128
+    (imaginary part 0): the overlap of real wavefunctions on the half basis."""
+    _check_block(X, "X")
+    _check_block(Y, "Y")
+    if X.dtype != Y.dtype or X.shape[0] != 1 or Y.shape[0] != 1 or X.shape[2] != Y.shape[2]:
+        raise ValueError(f"dot_real operands differ: {tuple(X.shape)} {X.dtype} vs {tuple(Y.shape)} {Y.dtype}")
+    _, nx, n_tot = X.shape
+    ny = Y.shape[1]
+    if out is None:
+        out = torch.empty((1, nx, ny), dtype=torch.complex128, device=X.device)
+    elif out.dtype != torch.complex128 or tuple(out.shape) != (1, nx, ny) or not out.is_contiguous():
+        raise ValueError("out must be a contiguous complex128 (1, nx, ny) tensor")
+    lib = _lib.lib()
+    ws = workspace(lib.qgb_dot_workspace_bytes(_qdtype(X), 1, nx, ny, n_tot), X.device)
+    _lib.check(lib.qgb_dot_real(_qdtype(X), X.data_ptr(), nx, Y.data_ptr(), ny, n_tot, _weight_ptr(weight, n_tot),
+                                out.data_ptr(), ws.data_ptr(), ws.numel(), _stream()), "dot_real")
+    return out
+
+
+def symmetrize_real(rb, X: torch.Tensor) -> torch.Tensor:
+    """In place: the Gz = 0 plane of X made Hermitian, c(G) = (c(G) + conj(c(-G))) / 2."""
+    nb = _check_real(rb, X, "X")
+    _lib.check(_lib.lib().qgb_symmetrize_real(rb.qdtype, ct.byref(rb.struct), X.data_ptr(), nb, _stream()),
+               "symmetrize_real")
+    return X
