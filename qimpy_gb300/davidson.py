@@ -12,6 +12,10 @@ eigenvalue change).  Additions:
   orthogonalisation of the expanded basis where its overlap is still too
   ill-conditioned for FP32 (directions below 1e-4 of the overlap dropped), and
   a stop at FP32's floor that leaves the rest to the FP64 refinement;
+* real (Gamma-point) wavefunctions (Basis(real=True)): weighted overlaps,
+  norms and kinetic energies, real subspace matrices and eigenvectors, and the
+  Gz = 0 plane symmetrised after every expansion (the reference's Davidson in
+  real-wavefunction mode, _basis_real.py with _wavefunction_dot.py:55-88);
 * ``refine_fp64``: FP64 refinement of a mixed-precision solve (Cholesky
   orthonormalisation, then FP64 Davidson sweeps: FP64 H.psi, Rayleigh-Ritz,
   residual expansion, expanded Rayleigh-Ritz).
@@ -73,6 +77,12 @@ def randomize_selected(C: Wavefunction, i_k: torch.Tensor, i_band: torch.Tensor,
     C._projT = None
 
 
+def _sub(M: torch.Tensor, real: bool) -> torch.Tensor:
+    """Subspace matrix as the eigensolver takes it: real wavefunctions' overlaps
+    are real (their imaginary parts are zero by construction)."""
+    return M.real.contiguous() if real else M
+
+
 def _tile_expansion(C_XC: torch.Tensor, Cnew_XCexp: torch.Tensor) -> torch.Tensor:
     """Expanded subspace matrix (qimpy/dft/electrons/_davidson.py:240-264)."""
     nk, n_new, n_exp = Cnew_XCexp.shape
@@ -108,7 +118,8 @@ class Davidson:
         one pass of qgb_residual (with zero eigenvalues, the residual of Cerr is Cerr)."""
         out = torch.empty_like(Cerr.coeff)
         zero = torch.zeros((Cerr.coeff.shape[0], Cerr.n_bands()), dtype=torch.float64, device=out.device)
-        ops.residual(Cerr.coeff, Cerr.coeff, zero, self.electrons.basis.ke, KEref, out=out)
+        ops.residual(Cerr.coeff, Cerr.coeff, zero, self.electrons.basis.ke, KEref, out=out,
+                     weight=self.electrons.basis.weight)
         return Wavefunction(Cerr.basis, coeff=out)
 
     def _regularize(self, C: Wavefunction, norm: torch.Tensor, i_iter: int) -> None:
@@ -146,8 +157,11 @@ class Davidson:
                 f"n_bands + n_bands_extra = {n_bands_max} exceeds min(n_basis)/2 = {el.basis.n_min // 2} in Davidson"
             )
         hpsi_bands = el.C.n_bands() * el.basis.nk
+        real = el.basis.real is not None
+        w = el.basis.weight
+        cdt = torch.float64 if real else torch.complex128
         HC = yield el.C
-        el.eig, V = eigh((el.C ^ HC).wait())  # _davidson.py:164-168
+        el.eig, V = eigh(_sub((el.C ^ HC).wait(), real))  # _davidson.py:164-168
         el.deig_max = np.inf
         el.C = el.C @ V
         HC = HC @ V
@@ -165,11 +179,11 @@ class Davidson:
             # (_davidson.py:177-183), in three band-wise passes: reference KE,
             # preconditioned residual (with its norm), then null-band
             # randomisation, normalisation and constrain; no host sync.
-            KEref = ops.band_norm_ke(el.C.coeff, basis.ke, b0=n_eigs_done, norm=False)[1]
+            KEref = ops.band_norm_ke(el.C.coeff, basis.ke, b0=n_eigs_done, norm=False, weight=w)[1]
             Cexp = Wavefunction(basis, coeff=torch.empty((basis.nk, n_bands_cur - n_eigs_done, basis.n_tot),
                                                          dtype=el.C.coeff.dtype, device=el.C.coeff.device))
             norm_exp = ops.residual(HC.coeff, el.C.coeff, el.eig, basis.ke, KEref, b0=n_eigs_done, out=Cexp.coeff,
-                                    norm=not fp32)
+                                    norm=not fp32, weight=w)
             if fp32:
                 # Project span(C) out of the expansion (twice: classical
                 # Gram-Schmidt with re-orthogonalisation).  span(C, Cexp) and
@@ -177,19 +191,21 @@ class Davidson:
                 # new directions are a small part of Cexp, and keeping the rest
                 # would leave the overlap too ill-conditioned for FP32.
                 for _ in range(2):
-                    ops.matmul(el.C.coeff, -ops.dot(el.C.coeff, Cexp.coeff), out=Cexp.coeff, accumulate=True)
+                    ops.matmul(el.C.coeff, -_sub((el.C ^ Cexp).wait(), real), out=Cexp.coeff, accumulate=True)
                 norm_exp = Cexp.band_norm()
             ops.normalize_bands(Cexp.coeff, basis.n_device, norm_exp, self._norm_cut, self._i_iter, basis.n_max,
                                 basis.ke)
+            if real:
+                ops.symmetrize_real(basis.real, Cexp.coeff)
             n_bands_exp = Cexp.n_bands()
             n_bands_new = n_bands_cur + n_bands_exp
             Cnew = el.C.cat(Cexp)
-            C_OC = torch.eye(n_bands_cur, device=V.device, dtype=torch.complex128)[None]
-            C_OC_new = _tile_expansion(C_OC, (Cnew ^ Cexp).wait())
+            C_OC = torch.eye(n_bands_cur, device=V.device, dtype=cdt)[None]
+            C_OC_new = _tile_expansion(C_OC, _sub((Cnew ^ Cexp).wait(), real))
             HCexp = yield Cexp
             hpsi_bands += n_bands_exp * el.basis.nk
-            C_HC = torch.diag_embed(el.eig).to(torch.complex128)
-            C_HC_new = _tile_expansion(C_HC, (Cnew ^ HCexp).wait())
+            C_HC = torch.diag_embed(el.eig).to(cdt)
+            C_HC_new = _tile_expansion(C_HC, _sub((Cnew ^ HCexp).wait(), real))
             # FP32 vectors: directions the expanded basis barely spans are below
             # its rounding and are dropped (canonical orthogonalisation).
             eig_new, V_new, failed = eighg(C_HC_new, C_OC_new, drop_below=1e-4 if fp32 else 0.0, check=False)
@@ -230,7 +246,7 @@ class Davidson:
                 # iterations; test residuals against a fresh H C.
                 HC = yield el.C
                 hpsi_bands += el.C.n_bands() * el.basis.nk
-                res = ops.residual(HC.coeff, el.C.coeff, el.eig, norm=True)
+                res = ops.residual(HC.coeff, el.C.coeff, el.eig, norm=True, weight=w)
                 res_max = float(res[:, :n_bands].max())
                 if res_max >= self.residual_threshold:
                     converged = False

@@ -14,6 +14,10 @@ Class and method names follow the reference so the eigensolver reads the same:
 
 Coefficients drop the reference's singleton spin and spinor axes (one spin
 channel, no spinors); ``Wavefunction.coeff5`` gives the reference's 5D view.
+``Basis(..., real=True)`` is the reference's real-wavefunction (Gamma-point)
+mode (qimpy/dft/electrons/_basis_real.py): coefficients on the half basis
+Gz >= 0, overlaps and norms weighted by 1 (Gz = 0) / 2, real overlap
+matrices, constrain symmetrising the Gz = 0 plane.
 Precision: ``complex128`` is the plain FP64 drop-in; ``complex64`` runs H.psi
 in FP32 while the subspace algebra (``dot`` results, ``eighg``) is FP64.
 """
@@ -43,7 +47,7 @@ class Basis:
     """Plane-wave basis of one cell at all its k-points, resident on one GPU."""
 
     def __init__(self, Rbasis, k, wk, ke_cutoff: float, grid_shape, device="cuda",
-                 dtype: torch.dtype = torch.complex128, fft_factors=None, layout=None):
+                 dtype: torch.dtype = torch.complex128, fft_factors=None, layout=None, real: bool = False):
         Rbasis = np.asarray(Rbasis, dtype=np.float64)
         self.Rbasis = Rbasis
         self.Gbasis = 2.0 * np.pi * np.linalg.inv(Rbasis.T)
@@ -54,6 +58,17 @@ class Basis:
         self.grid_shape = tuple(int(x) for x in grid_shape)
         self.device = torch.device(device)
         self.dtype = dtype
+        self.real = None  #: DeviceRealBasis of the real-wavefunction mode
+        self.weight = None  #: FP64 overlap weights of the half basis (real mode)
+        if real:
+            from .real_basis import DeviceRealBasis, gamma_bases
+
+            if self.k.shape[0] != 1 or np.any(self.k != 0.0):
+                raise ValueError("real wavefunctions need the Gamma point alone")
+            half, full = gamma_bases(self.Gbasis, self.ke_cutoff, self.grid_shape)
+            self.real = DeviceRealBasis(half, full, self.device, dtype, fft_factors)
+            self.weight = self.real.weight
+            layout = half
         self.layout = layout or wl.make_basis(self.Gbasis, self.k, self.ke_cutoff, self.grid_shape)
         self.n = self.layout.n
         self.n_tot = self.layout.n_tot
@@ -61,8 +76,12 @@ class Basis:
         self.n_max = int(self.n.max())
         self.fft_index = self.layout.fft_index
         self.iG = self.layout.iG
-        self.tables = sp.build_tables(self.fft_index, self.n, self.grid_shape, fft_factors)
-        self.sphere = sp.DeviceSphere(self.tables, self.layout.ke, self.device, dtype)
+        if self.real is None:
+            self.tables = sp.build_tables(self.fft_index, self.n, self.grid_shape, fft_factors)
+            self.sphere = sp.DeviceSphere(self.tables, self.layout.ke, self.device, dtype)
+        else:  # transforms run on the full Gamma sphere
+            self.sphere = self.real.sphere
+            self.tables = self.sphere.tables
         self.ke = torch.from_numpy(self.layout.ke).to(self.device)  # FP64 always
         pad = torch.arange(self.n_tot)[None, :] < torch.from_numpy(self.n)[:, None]
         self.mask = pad.to(self.device)  # True inside the sphere
@@ -92,13 +111,20 @@ class Basis:
 
     def apply_ke(self, C: "Wavefunction") -> "Wavefunction":
         """KE * C (qimpy/dft/electrons/_basis_ops.py:29-36) on the GPU."""
+        self._complex_only("apply_ke")
         return Wavefunction(self, coeff=ops.apply_ke(self.sphere, C.coeff))
 
     def apply_potential(self, V, C: "Wavefunction") -> "Wavefunction":
         """V * C on the G-sphere (qimpy/dft/electrons/_basis_ops.py:39-113)."""
+        self._complex_only("apply_potential")
         if V is not None and id(V) != self._V_id:
             self.set_potential(V)
         return Wavefunction(self, coeff=ops.apply_potential(self.sphere, C.coeff))
+
+    def _complex_only(self, what: str) -> None:
+        if self.real is not None:
+            raise NotImplementedError(f"{what} of real wavefunctions runs inside Electrons.hamiltonian "
+                                      "(qgb_hamiltonian_real)")
 
     def collect_density(self, C: "Wavefunction", f: torch.Tensor, need_Mvec: bool = False) -> torch.Tensor:
         """Electron density (qimpy/dft/electrons/_basis_ops.py:207-296) of the bands
@@ -107,6 +133,7 @@ class Basis:
         reference's FieldR data with its one density component)."""
         if need_Mvec:
             raise NotImplementedError("magnetization densities need spinorial wavefunctions")
+        self._complex_only("collect_density")
         f = f.reshape(C.coeff.shape[0], C.n_bands()).to(torch.float64)
         w_sk = 2.0 * torch.from_numpy(self.wk).to(f.device)
         prefac = f * (w_sk[:, None] / self.volume)
@@ -128,7 +155,8 @@ class Ions:
             self.n_projectors = int(beta.shape[1])
         # Mixed form: bf16 hi/lo projector operands for the tensor-core GEMMs.
         self.beta_split = (ops.beta_split(self.beta)
-                           if self.beta is not None and basis.dtype == torch.complex64 else None)
+                           if self.beta is not None and basis.dtype == torch.complex64 and basis.real is None
+                           else None)
         self.beta_version = 0
 
     def D_all(self) -> torch.Tensor:
@@ -179,7 +207,10 @@ class Wavefunction:
     # --- algebra --------------------------------------------------------------
     def dot(self, other: "Wavefunction") -> Waitless:
         """[k, b1, b2] = sum_g conj(self) other (qimpy/dft/electrons/_wavefunction_dot.py:18-107);
-        FP64 result for both precisions (qgb_dot)."""
+        FP64 result for both precisions (qgb_dot).  Real wavefunctions: weighted
+        and imaginary part zero (qgb_dot_real)."""
+        if self.basis.real is not None:
+            return Waitless(ops.dot_real(self.coeff, other.coeff, self.basis.weight))
         return Waitless(ops.dot(self.coeff, other.coeff))
 
     __xor__ = dot
@@ -196,15 +227,18 @@ class Wavefunction:
 
     def band_norm(self) -> torch.Tensor:
         """sqrt(sum_g |c|^2), FP64 (qimpy/dft/electrons/_wavefunction.py:226-236; qgb_band_norm_ke)."""
-        return ops.band_norm_ke(self.coeff)[0]
+        return ops.band_norm_ke(self.coeff, weight=self.basis.weight)[0]
 
     def band_ke(self) -> torch.Tensor:
         """sum_g |c|^2 KE, FP64 (qimpy/dft/electrons/_wavefunction.py:238-247; qgb_band_norm_ke)."""
-        return ops.band_norm_ke(self.coeff, self.basis.ke, norm=False)[1]
+        return ops.band_norm_ke(self.coeff, self.basis.ke, norm=False, weight=self.basis.weight)[1]
 
     def constrain(self) -> None:
-        """Zero padded coefficients (qimpy/dft/electrons/_wavefunction.py:264-275)."""
+        """Zero padded coefficients (qimpy/dft/electrons/_wavefunction.py:264-275);
+        real wavefunctions: Gz = 0 plane made Hermitian (BasisReal.symmetrize)."""
         self.coeff.mul_(self.basis.mask[:, None, :])
+        if self.basis.real is not None:
+            ops.symmetrize_real(self.basis.real, self.coeff)
         self._projT = None
 
     def cat(self, other: "Wavefunction") -> "Wavefunction":
@@ -213,7 +247,8 @@ class Wavefunction:
     def orthonormalize(self) -> "Wavefunction":
         from .linalg import ortho_matrix
 
-        return self @ ortho_matrix(self.dot(self).wait())
+        O = self.dot(self).wait()
+        return self @ ortho_matrix(O.real if self.basis.real is not None else O)
 
     def __mul__(self, scale):
         if isinstance(scale, torch.Tensor) and scale.dim() == 2:  # per (k, band)
@@ -270,7 +305,10 @@ class Electrons:
         """HC in one C-ABI call: fused KE + local potential, then the nonlocal
         term (FP64: ZGEMMs; mixed: tcgen05 split-BF16x3 GEMMs)."""
         ions = self.ions
-        if self.basis.dtype == torch.complex64:
+        if self.basis.real is not None:
+            beta = ions.beta if ions.n_projectors else None
+            HC, projT = ops.hamiltonian_real(self.basis.real, C.coeff, beta, ions.D)
+        elif self.basis.dtype == torch.complex64:
             HC, projT = ops.hamiltonian_mixed(self.basis.sphere, C.coeff, ions.beta_split, ions.D)
         else:
             beta = ions.beta if ions.n_projectors else None
@@ -281,10 +319,11 @@ class Electrons:
         return Wavefunction(self.basis, coeff=HC)
 
 
-def from_problem(prob: wl.Problem, device="cuda", dtype=torch.complex128, n_bands_total: Optional[int] = None):
-    """Build (electrons, C0) for a synthetic problem; C0 is orthonormalised like
-    Electrons.initialize_wavefunctions does (qimpy/dft/electrons/_electrons.py:287)."""
-    basis = Basis(prob.Rbasis, prob.k, prob.wk, prob.ke_cutoff, prob.grid_shape, device, dtype)
+def from_problem(prob: wl.Problem, device="cuda", dtype=torch.complex128, n_bands_total: Optional[int] = None,
+                 real: bool = False):
+    """Build (electrons, C0) for a synthetic problem (real=True: real
+    wavefunctions on the half basis, Gamma-only problems)."""
+    basis = Basis(prob.Rbasis, prob.k, prob.wk, prob.ke_cutoff, prob.grid_shape, device, dtype, real=real)
     beta = torch.from_numpy(wl.make_projectors(prob, basis.layout))
     ions = Ions(basis, beta, torch.from_numpy(prob.D_atom).to(torch.complex128))
     el = Electrons(basis, ions, torch.from_numpy(prob.V_r), prob.n_bands, prob.n_bands_extra)

@@ -23,8 +23,13 @@ def eigh(A: torch.Tensor, check: bool = True):
     converge (as torch.linalg.eigh does); with check=False it returns
     (E, V, failed) instead, `failed` a device bool per matrix, without the host
     synchronisation the check needs."""
-    if A.device.type != "cuda" or A.dtype != torch.complex128:
-        raise TypeError(f"eigh needs complex128 CUDA matrices, got {A.dtype} on {A.device}")
+    if A.device.type != "cuda" or A.dtype not in (torch.complex128, torch.float64):
+        raise TypeError(f"eigh needs complex128 or float64 CUDA matrices, got {A.dtype} on {A.device}")
+    if A.dtype == torch.float64:
+        # Real symmetric (the overlaps of real wavefunctions): real eigenvectors,
+        # so that rotations keep the bands real.  cuSOLVER through torch.linalg.
+        W, V = torch.linalg.eigh(A)
+        return (W, V) if check else (W, V, torch.zeros(A.shape[:-2], dtype=torch.bool, device=A.device))
     n = A.shape[-1]
     lead = A.shape[:-2]
     X = A.reshape(-1, n, n).clone(memory_format=torch.contiguous_format)
