@@ -349,6 +349,37 @@ int qgb_hamiltonian_real(const qgb_sphere* full, const qgb_real_map* map, int dt
 int qgb_symmetrize_real(int dtype, const qgb_real_map* map, void* X, int nb, void* stream);
 
 /*
+ * Projectors generated on the device (replaces Ions.get_projectors,
+ * qimpy/dft/ions/_ions_projectors.py:14-72):
+ *   beta[k][a pa + j][g] = i^l S_lm(q) R_s(|q|) exp(-2 pi i (iG + k).tau_a) / sqrt(volume),
+ *   q = (iG + k) Gbasis^T,
+ * for atoms a (fractional positions [n_atoms][3], FP64, device) and the atom
+ * template of `shells` (host array; projector j runs over the shells in order
+ * and, within a shell, over the 2l + 1 real solid harmonics S_lm = |q|^l Y_lm,
+ * m = -l..l, l = 1 as (y, z, x); pa = sum (2l + 1)).  Radial R_s:
+ *   QGB_RADIAL_GAUSSIAN  (-1)^l (2 pi)^{3/2} sigma^{2l+3} exp(-sigma^2 |q|^2 / 2), the
+ *                        transform of r^l Y_lm exp(-r^2 / (2 sigma^2))
+ *   QGB_RADIAL_BLIP      quintic blip spline with coefficients coeff[n_coeff]
+ *                        (FP64, device) on spacing dq, evaluated as the
+ *                        reference's Interpolator (qimpy/math/quintic_spline.py:57-130)
+ * iG int32 [nk][n_tot][3], k FP64 [nk][3] and n int32 [nk] on the device;
+ * Gbasis FP64 [3][3] row-major on the host.  beta [nk][n_atoms pa][n_tot] of
+ * `dtype` (computed in FP64); entries g >= n[k] are zero.  l <= 2, at most 8 shells.
+ */
+enum qgb_radial_kind { QGB_RADIAL_GAUSSIAN = 0, QGB_RADIAL_BLIP = 1 };
+typedef struct qgb_projector_shell {
+  int32_t l;
+  int32_t kind;         /* enum qgb_radial_kind */
+  double sigma;         /* QGB_RADIAL_GAUSSIAN: width (bohr) */
+  const double* coeff;  /* QGB_RADIAL_BLIP: blip coefficients (device) */
+  int32_t n_coeff;
+  double dq;            /* QGB_RADIAL_BLIP: |q| spacing of the coefficients */
+} qgb_projector_shell;
+int qgb_make_projectors(int dtype, int nk, int n_tot, const int32_t* n, const int32_t* iG, const double* k,
+                        const double* Gbasis, int n_atoms, const double* positions, int n_shells,
+                        const qgb_projector_shell* shells, double volume, void* beta, void* stream);
+
+/*
  * Mixed-precision nonlocal term on the tcgen05 tensor cores (split-BF16x3,
  * FP32 accumulation):  projT = <beta|C>  and  HC += beta (D projT), complex64
  * (replaces C.proj and beta @ (D_all @ C.proj),

@@ -42,6 +42,16 @@ class QgbRealMap(ct.Structure):
                 ("plane", ct.c_void_p), ("ke", ct.c_void_p), ("weight", ct.c_void_p)]
 
 
+class QgbProjectorShell(ct.Structure):
+    """Mirror of ``struct qgb_projector_shell``."""
+
+    _fields_ = [("l", ct.c_int32), ("kind", ct.c_int32), ("sigma", ct.c_double), ("coeff", ct.c_void_p),
+                ("n_coeff", ct.c_int32), ("dq", ct.c_double)]
+
+
+QGB_RADIAL_GAUSSIAN, QGB_RADIAL_BLIP = 0, 1
+
+
 class QgbBatchItem(ct.Structure):
     """Mirror of ``struct qgb_batch_item``."""
 
@@ -86,6 +96,9 @@ _SIGS = {
                                         ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
                                         ct.c_void_p, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
     "qgb_symmetrize_real": (ct.c_int, [ct.c_int, ct.POINTER(QgbRealMap), ct.c_void_p, ct.c_int, ct.c_void_p]),
+    "qgb_make_projectors": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                       ct.POINTER(ct.c_double), ct.c_int, ct.c_void_p, ct.c_int,
+                                       ct.POINTER(QgbProjectorShell), ct.c_double, ct.c_void_p, ct.c_void_p]),
     "qgb_matmul": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int,
                               ct.c_void_p, ct.c_uint, ct.c_void_p]),
     "qgb_apply_nonlocal": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p,

@@ -132,24 +132,12 @@ class Instance:
         return V
 
     def _projectors(self, dev, Gb):
-        """s + p Gaussian projectors (sigma 1) on every atom, D = diag(1.5, -0.8 x3)."""
+        """s + p Gaussian projectors (sigma 1) on every atom, generated on the
+        device (qgb_make_projectors); D = diag(1.5, -0.8 x3)."""
         lay = self.layout
-        iG = torch.from_numpy(lay.iG).to(dev, torch.float64)
-        k = torch.from_numpy(self.spec.k).to(dev, torch.float64)
-        kiG = iG + k[:, None, :]
-        q = kiG @ torch.from_numpy(Gb.T).to(dev)
-        q2 = q.square().sum(-1)
-        rad = ((2 * math.pi) ** 1.5 * torch.exp(-0.5 * q2)).to(torch.complex128)
-        c1 = -1j * math.sqrt(3 / (4 * math.pi))
-        ang = torch.stack((torch.full_like(rad, 0.5 / math.sqrt(math.pi)),
-                           c1 * q[..., 1].to(torch.complex128),
-                           c1 * q[..., 2].to(torch.complex128),
-                           c1 * q[..., 0].to(torch.complex128)), dim=1) * rad[:, None, :]
-        pos = torch.from_numpy(self.spec.positions).to(dev, torch.float64)
-        phase = torch.exp(-2j * math.pi * torch.einsum("kgx,ax->kag", kiG, pos)) / math.sqrt(self.volume)
-        beta = (ang[:, None, :, :] * phase[:, :, None, :]).reshape(self.nk, -1, lay.n_tot)
-        mask = torch.arange(lay.n_tot, device=dev)[None, :] < torch.from_numpy(lay.n).to(dev)[:, None]
-        beta = (beta * mask[:, None, :]).to(self.dtype).contiguous()
+        shells = [(0, ("gauss", 1.0)), (1, ("gauss", 1.0))]
+        beta = ops.make_projectors(lay.iG, self.spec.k, Gb, lay.n, self.spec.positions, shells, self.volume,
+                                   self.dtype, dev)
         D = torch.diag(torch.tensor([1.5, -0.8, -0.8, -0.8], dtype=self.dtype, device=dev))
         return beta, D.expand(self.spec.n_atoms, 4, 4).contiguous()
 

@@ -324,7 +324,7 @@ def from_problem(prob: wl.Problem, device="cuda", dtype=torch.complex128, n_band
     """Build (electrons, C0) for a synthetic problem (real=True: real
     wavefunctions on the half basis, Gamma-only problems)."""
     basis = Basis(prob.Rbasis, prob.k, prob.wk, prob.ke_cutoff, prob.grid_shape, device, dtype, real=real)
-    beta = torch.from_numpy(wl.make_projectors(prob, basis.layout))
+    beta = wl.make_projectors_device(prob, basis.layout, basis.device, dtype)  # qgb_make_projectors
     ions = Ions(basis, beta, torch.from_numpy(prob.D_atom).to(torch.complex128))
     el = Electrons(basis, ions, torch.from_numpy(prob.V_r), prob.n_bands, prob.n_bands_extra)
     nbt = n_bands_total or (prob.n_bands + prob.n_bands_extra)

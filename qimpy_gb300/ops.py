@@ -438,3 +438,46 @@ def symmetrize_real(rb, X: torch.Tensor) -> torch.Tensor:
     _lib.check(_lib.lib().qgb_symmetrize_real(rb.qdtype, ct.byref(rb.struct), X.data_ptr(), nb, _stream()),
                "symmetrize_real")
     return X
+
+
+# ---------------------------------------------------------------------------
+# Projectors generated on the device
+# ---------------------------------------------------------------------------
+
+
+def make_projectors(iG, k, Gbasis, n, positions, shells, volume: float, dtype: torch.dtype, device) -> torch.Tensor:
+    """beta (nk, n_atoms pa, n_tot) of `dtype` on `device` (qgb_make_projectors,
+    replacing Ions.get_projectors): iG (nk, n_tot, 3) integer, k (nk, 3) and
+    positions (n_atoms, 3) fractional, n (nk,) sphere sizes; shells a list of
+    (l, ("gauss", sigma)) or (l, ("blip", coeff, dq)) with coeff the radial
+    function's blip coefficients (1D, FP64) on |q| spacing dq."""
+    dev = torch.device(device)
+    iG_d = torch.as_tensor(iG).to(dev, torch.int32).contiguous()
+    nk, n_tot = int(iG_d.shape[0]), int(iG_d.shape[1])
+    if iG_d.dim() != 3 or iG_d.shape[2] != 3:
+        raise ValueError("iG must be (nk, n_tot, 3)")
+    k_d = torch.as_tensor(k, dtype=torch.float64).to(dev).reshape(nk, 3).contiguous()
+    n_d = torch.as_tensor(n).to(dev, torch.int32).reshape(nk).contiguous()
+    pos_d = torch.as_tensor(positions, dtype=torch.float64).to(dev).reshape(-1, 3).contiguous()
+    arr = (_lib.QgbProjectorShell * max(len(shells), 1))()
+    keep = []
+    for s, (l, (kind, *par)) in enumerate(shells):
+        arr[s].l = int(l)
+        if kind == "gauss":
+            arr[s].kind, arr[s].sigma = _lib.QGB_RADIAL_GAUSSIAN, float(par[0])
+        elif kind == "blip":
+            c = torch.as_tensor(par[0], dtype=torch.float64).to(dev).contiguous()
+            keep.append(c)
+            arr[s].kind, arr[s].coeff, arr[s].n_coeff, arr[s].dq = _lib.QGB_RADIAL_BLIP, c.data_ptr(), c.numel(), \
+                float(par[1])
+        else:
+            raise ValueError(f"unknown radial kind {kind!r}")
+    pa = sum(2 * int(l) + 1 for l, _ in shells)
+    beta = torch.empty((nk, pos_d.shape[0] * pa, n_tot), dtype=dtype, device=dev)
+    Gb = (ct.c_double * 9)(*[float(x) for x in torch.as_tensor(Gbasis, dtype=torch.float64).reshape(-1)])
+    with torch.cuda.device(dev):
+        _lib.check(_lib.lib().qgb_make_projectors(_qdtype(beta), nk, n_tot, n_d.data_ptr(), iG_d.data_ptr(),
+                                                  k_d.data_ptr(), Gb, pos_d.shape[0], pos_d.data_ptr(), len(shells),
+                                                  arr, float(volume), beta.data_ptr(), _stream()),
+                   "make_projectors")
+    return beta

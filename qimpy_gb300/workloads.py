@@ -335,6 +335,16 @@ def make_projectors(prob: Problem, basis: BasisLayout) -> np.ndarray:
     return beta
 
 
+def make_projectors_device(prob: Problem, basis: BasisLayout, device, dtype):
+    """``make_projectors`` generated on the device by qgb_make_projectors (the
+    same analytic Gaussian shells, computed in FP64, stored as `dtype`)."""
+    from . import ops
+
+    shells = [(sh.l, ("gauss", sh.sigma)) for sh in prob.shells]
+    return ops.make_projectors(basis.iG, prob.k, prob.Gbasis, basis.n, prob.positions, shells, prob.volume,
+                               dtype, device)
+
+
 def make_wavefunctions(prob: Problem, basis: BasisLayout, n_bands: int, seed_stream: int = 7,
                        band_offset: int = 0) -> np.ndarray:
     """C0[k, b, g] = complex Gaussian / (1 + |k+G|^2 / 2); padding zero.

@@ -301,6 +301,54 @@ def run_real_case(qimpy, name: str, out_dir: str) -> None:
     print(f"real {name}: wrote {path}")
 
 
+#: workloads whose projectors are also made by the reference's own
+#: Ions.get_projectors (blip-spline radial tables of the Gaussian shells)
+PROJECTOR_CASES = ("tiny_fcc", "tiny_gamma")
+PROJECTOR_DG = 0.02  # the reference's radial spline spacing (qimpy/math/_radial_function.py:22)
+
+
+def run_projector_case(qimpy, name: str, out_dir: str) -> None:
+    """beta from the unmodified Ions.get_projectors
+    (qimpy/dft/ions/_ions_projectors.py:14-72), called with a stand-in for the
+    ions object that supplies what it reads: one species on the workload's
+    atoms whose radial functions are the workload's Gaussian shells, sampled
+    on the reference's spline spacing and converted with its get_coeff."""
+    import torch
+    from qimpy.dft.ions import _ions_projectors as ip
+    from qimpy.dft.ions._ions import Ions
+    from qimpy.math import quintic_spline
+
+    prob = wl.get(name)
+    real = bool(prob.extra.get("real_wavefunctions", False))
+    system = build_system(qimpy, prob, None, real=real)
+    basis = system.electrons.basis
+    iGk = basis.iG + basis.k[:, None]
+    qmax = float(((iGk @ torch.from_numpy(prob.Gbasis).T) ** 2).sum(-1).sqrt().max())
+    nG = int(np.ceil(qmax / PROJECTOR_DG)) + 5
+    q = np.arange(nG) * PROJECTOR_DG
+    samples = np.stack([(-1.0) ** sh.l * (2 * np.pi) ** 1.5 * sh.sigma ** (2 * sh.l + 3)
+                        * np.exp(-0.5 * sh.sigma ** 2 * q ** 2) for sh in prob.shells])
+    coeff = quintic_spline.get_coeff(torch.from_numpy(samples))  # (nG + 4, n_shells)
+    i_rf, i_lm = [], []
+    for s, sh in enumerate(prob.shells):
+        for m in range(2 * sh.l + 1):
+            i_rf.append(s)
+            i_lm.append(sh.l * sh.l + m)
+    pqn = types.SimpleNamespace(n_tot=len(i_rf), i_rf=torch.tensor(i_rf), i_lm=torch.tensor(i_lm))
+    ps = types.SimpleNamespace(l_max=max(sh.l for sh in prob.shells), pqn_beta=pqn,
+                               beta=types.SimpleNamespace(f_tilde_coeff=coeff))
+    ions = types.SimpleNamespace(
+        lattice=types.SimpleNamespace(Gbasis=torch.from_numpy(prob.Gbasis), volume=prob.volume),
+        positions=torch.from_numpy(prob.positions), n_projectors=prob.n_projectors, pseudopotentials=[ps],
+        n_ions_type=[prob.n_atoms], slices=[slice(0, prob.n_atoms)])
+    ions.translation_phase = lambda iG, atom_slice=slice(None): Ions.translation_phase(ions, iG, atom_slice)
+    beta = ip.get_projectors(ions, basis, full_basis=True).coeff[0, :, :, 0, :].numpy()
+    path = os.path.join(out_dir, f"projectors_{name}.npz")
+    np.savez_compressed(path, beta=beta, coeff=coeff.numpy().T.copy(), dq=PROJECTOR_DG,
+                        fft_index=basis.fft_index.numpy())
+    print(f"projectors {name}: wrote {path}")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
@@ -309,9 +357,10 @@ def main() -> None:
     ap.add_argument("--chefsi", action="store_true", help="only the CheFSI goldens")
     ap.add_argument("--density", action="store_true", help="only the density goldens")
     ap.add_argument("--real", action="store_true", help="only the real-wavefunction goldens")
+    ap.add_argument("--projectors", action="store_true", help="only the projector goldens")
     args = ap.parse_args()
     qimpy = import_reference(args.ref)
-    only_part = args.chefsi or args.density or args.real
+    only_part = args.chefsi or args.density or args.real or args.projectors
     for name, cfg in CASES.items():
         if only_part or (args.only and name not in args.only):
             continue
@@ -328,6 +377,10 @@ def main() -> None:
         if (only_part and not args.real) or (args.only and name not in args.only):
             continue
         run_real_case(qimpy, name, args.out)
+    for name in PROJECTOR_CASES:
+        if (only_part and not args.projectors) or (args.only and name not in args.only):
+            continue
+        run_projector_case(qimpy, name, args.out)
 
 
 if __name__ == "__main__":

@@ -189,3 +189,33 @@ def test_oracle_real_wavefunction_chefsi_matches_reference():
     assert r.converged
     assert np.abs(r.eig[:, : p.n_bands] - g["chefsi_eig"][:, : p.n_bands]).max() < 1e-10
     assert r.iterations == int(g["chefsi_iterations"])
+
+
+@pytest.mark.parametrize("name", ["tiny_fcc", "tiny_gamma"])
+def test_oracle_projectors_match_reference(name):
+    """The oracle's projector construction against the reference's own
+    Ions.get_projectors (tests/golden/projectors_*.npz): the blip coefficients
+    of the Gaussian shells' radial samples (get_coeff), beta from those tables
+    (Interpolator, harmonics with the i^l phase, translation phases), and the
+    analytic-radial form against the workloads' projectors, which the spline
+    approximates to ~1e-9."""
+    from oracle import projectors as op
+
+    g = np.load(os.path.join(GOLDEN, f"projectors_{name}.npz"))
+    p = wl.get(name)
+    b = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape, real=bool(p.extra.get("real_wavefunctions")))
+    assert np.array_equal(b.fft_index, g["fft_index"])
+    dq = float(g["dq"])
+    q = np.arange(g["coeff"].shape[1] - 4) * dq
+    for s, sh in enumerate(p.shells):
+        samples = (-1.0) ** sh.l * (2 * np.pi) ** 1.5 * sh.sigma ** (2 * sh.l + 3) * np.exp(-0.5 * sh.sigma ** 2 * q ** 2)
+        c = op.blip_coeff(samples)
+        assert np.abs(c - g["coeff"][s]).max() <= 1e-14 * np.abs(g["coeff"][s]).max()
+    blip = [(sh.l, ("blip", g["coeff"][s], dq)) for s, sh in enumerate(p.shells)]
+    gauss = [(sh.l, ("gauss", sh.sigma)) for sh in p.shells]
+    beta_b = op.projectors(b.iG, p.k, p.Gbasis, b.n, p.positions, blip, p.volume)
+    beta_g = op.projectors(b.iG, p.k, p.Gbasis, b.n, p.positions, gauss, p.volume)
+    ref = g["beta"]
+    assert np.abs(beta_b - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.abs(beta_g - wl.make_projectors(p, b)).max() <= 1e-14 * np.abs(ref).max()
+    assert np.abs(beta_g - ref).max() <= 1e-8 * np.abs(ref).max()
