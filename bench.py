@@ -614,12 +614,15 @@ def run_eigensolve_si64(args, local):
 def run_real_hpsi(args, local):
     """H.psi of real (Gamma-point) wavefunctions on the half basis of the
     64-atom Si cell (96^3, n_half = 18,561 of the 37,073-point sphere,
-    P = 256), 160 bands in blocks of 32, FP64 and FP32, through
-    qgb_hamiltonian_real (two real bands per complex transform).  Same timing
+    P = 256), 160 bands in blocks of 32, FP64 (qgb_hamiltonian_real) and mixed
+    (qgb_hamiltonian_real_mixed: FP32 local potential, tensor-core nonlocal);
+    two real bands per complex transform.  Same timing
     rules as the headline: CUDA events per step, 512 MB L2 flush between steps."""
     import torch
 
-    from qimpy_gb300 import ops, real_basis as rbm, workloads as wl
+    import ctypes as ct
+
+    from qimpy_gb300 import _lib, ops, real_basis as rbm, workloads as wl
 
     dev = torch.device(f"cuda:{local}")
     p = wl.get("si64")
@@ -637,12 +640,22 @@ def run_real_hpsi(args, local):
         D = torch.from_numpy(p.D_atom).to(dev, cdt)
         blocks = [C[:, s:s + block].contiguous() for s in range(0, nb, block)]
         outs = [torch.empty_like(c) for c in blocks]
-        projT = torch.empty((1, block, beta.shape[1]), dtype=cdt, device=dev)
-        ws = ops.workspace(rb.workspace_bytes(block, beta.shape[1]), dev)
+        P = beta.shape[1]
+        projT = torch.empty((1, block, P), dtype=cdt, device=dev)
+        mixed = cdt == torch.complex64
+        if mixed:  # tensor-core nonlocal (qgb_hamiltonian_real_mixed)
+            split = ops.beta_split(beta)
+            ws = ops.workspace(_lib.lib().qgb_hamiltonian_real_mixed_workspace_bytes(
+                ct.byref(rb.sphere.struct), ct.byref(rb.struct), block, P), dev)
+        else:
+            ws = ops.workspace(rb.workspace_bytes(block, P), dev)
 
         def step():
             for c, o in zip(blocks, outs):
-                ops.hamiltonian_real(rb, c, beta, D, out=o, projT=projT[:, : c.shape[1]], ws=ws)
+                if mixed:
+                    ops.hamiltonian_real_mixed(rb, c, split, D, out=o, projT=projT[:, : c.shape[1]], ws=ws)
+                else:
+                    ops.hamiltonian_real(rb, c, beta, D, out=o, projT=projT[:, : c.shape[1]], ws=ws)
 
         for _ in range(args.warmup):
             step()

@@ -343,6 +343,18 @@ int qgb_hamiltonian_real(const qgb_sphere* full, const qgb_real_map* map, int dt
                          size_t workspace_bytes, void* stream);
 
 /*
+ * The same in the mixed form (complex64, FP32 local potential): the weighted
+ * real projection and the back-projection as tcgen05 split-BF16x3 GEMMs on
+ * qgb_beta_split operands of beta [1][P][n_tot_half] (the mixed counterpart
+ * of qgb_hamiltonian_real, as qgb_hamiltonian_mixed is of qgb_hamiltonian).
+ * dev_error as for qgb_apply_nonlocal_tc.
+ */
+size_t qgb_hamiltonian_real_mixed_workspace_bytes(const qgb_sphere* full, const qgb_real_map* map, int nb, int P);
+int qgb_hamiltonian_real_mixed(const qgb_sphere* full, const qgb_real_map* map, const void* C, void* HC, int nb,
+                               const void* beta_split, const void* D, int n_atoms, int pa, void* projT,
+                               void* workspace, size_t workspace_bytes, int* dev_error, void* stream);
+
+/*
  * X [nb][n_tot_half] in place: c(G) = (c(G) + conj(c(-G))) / 2 on the Gz = 0
  * plane (replaces BasisReal.symmetrize, qimpy/dft/electrons/_basis_real.py:68-106).
  */

@@ -95,6 +95,11 @@ _SIGS = {
     "qgb_hamiltonian_real": (ct.c_int, [ct.POINTER(QgbSphere), ct.POINTER(QgbRealMap), ct.c_int, ct.c_void_p,
                                         ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
                                         ct.c_void_p, ct.c_void_p, ct.c_size_t, ct.c_void_p]),
+    "qgb_hamiltonian_real_mixed_workspace_bytes": (ct.c_size_t, [ct.POINTER(QgbSphere), ct.POINTER(QgbRealMap),
+                                                                 ct.c_int, ct.c_int]),
+    "qgb_hamiltonian_real_mixed": (ct.c_int, [ct.POINTER(QgbSphere), ct.POINTER(QgbRealMap), ct.c_void_p, ct.c_void_p,
+                                              ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p,
+                                              ct.c_void_p, ct.c_size_t, ct.c_void_p, ct.c_void_p]),
     "qgb_symmetrize_real": (ct.c_int, [ct.c_int, ct.POINTER(QgbRealMap), ct.c_void_p, ct.c_int, ct.c_void_p]),
     "qgb_make_projectors": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                        ct.POINTER(ct.c_double), ct.c_int, ct.c_void_p, ct.c_int,

@@ -45,11 +45,13 @@ __device__ __forceinline__ void cmac(cplx_t<T>& acc, const cplx_t<T>& a, const c
 // Gram / projection: out(i, j) = sum_g conj(A[i][g]) B[j][g]
 // ---------------------------------------------------------------------------
 //
-// CTA: 64 (i) x 64 (j) outputs of one k and one g range (split-K), 256
-// threads as 16 x 16, each 4 x 4 outputs.  g is staged 16 at a time: A and B
-// tiles are loaded along g (coalesced rows) and stored transposed, [g][i] and
-// [g][j], so each thread reads 4 consecutive i (or j) per g.
-constexpr int GT = 64;   // i and j tile
+// CTA: BI (i) x BJ (j) outputs of one k and one g range (split-K), 256
+// threads as TI x TJ (TI TJ = 256), each 4 x 4 outputs: 64 x 64 in general,
+// 128 x 32 or 32 x 128 when one side has at most 32 rows (the projections of
+// a 32-band block), so that no thread multiplies padding.  g is staged 16 at a
+// time: A and B tiles are loaded along g (coalesced rows) and stored
+// transposed, [g][i] and [g][j], so each thread reads 4 consecutive i (or j)
+// per g.
 constexpr int GK = 16;   // g per stage
 constexpr int GPAD = 1;  // row padding (elements) of the transposed tiles
 
@@ -68,14 +70,15 @@ struct GramArgs {
   int real_out;                // keep only the real part (imaginary part written as 0)
 };
 
-template <typename T, typename OutT>
+template <typename T, typename OutT, int TI>
 __global__ void __launch_bounds__(256) k_gram(const GramArgs a) {
   using C2 = cplx_t<T>;
   using O2 = cplx_t<OutT>;
-  __shared__ C2 As[GK][GT + GPAD];
-  __shared__ C2 Bs[GK][GT + GPAD];
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
+  constexpr int TJ = 256 / TI, BI = 4 * TI, BJ = 4 * TJ;
+  __shared__ C2 As[GK][BI + GPAD];
+  __shared__ C2 Bs[GK][BJ + GPAD];
+  const int tid = threadIdx.x, tx = tid % TJ, ty = tid / TJ;
+  const int i0 = blockIdx.x * BI, j0 = blockIdx.y * BJ;
   const int k = blockIdx.z / a.splits, split = blockIdx.z % a.splits;
   const int g_begin = split * a.g_per_split;
   const int g_end = min(a.K, g_begin + a.g_per_split);
@@ -88,10 +91,15 @@ __global__ void __launch_bounds__(256) k_gram(const GramArgs a) {
     for (int q = 0; q < 4; ++q) acc[p][q] = mk<T>(T(0), T(0));
   for (int g0 = g_begin; g0 < g_end; g0 += GK) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < BI * GK / 256; ++r) {
+      const int e = tid + 256 * r, row = e >> 4, gg = e & 15, g = g0 + gg;
+      As[gg][row] = (g < g_end && i0 + row < a.M) ? A[static_cast<long long>(i0 + row) * a.lda + g]
+                                                  : mk<T>(T(0), T(0));
+    }
+#pragma unroll
+    for (int r = 0; r < BJ * GK / 256; ++r) {
       const int e = tid + 256 * r, row = e >> 4, gg = e & 15, g = g0 + gg;
       const bool g_ok = g < g_end;
-      As[gg][row] = (g_ok && i0 + row < a.M) ? A[static_cast<long long>(i0 + row) * a.lda + g] : mk<T>(T(0), T(0));
       C2 bv = (g_ok && j0 + row < a.N) ? B[static_cast<long long>(j0 + row) * a.ldb + g] : mk<T>(T(0), T(0));
       if (a.weight != nullptr && g_ok) {
         const T w = static_cast<T>(a.weight[g]);
@@ -168,13 +176,16 @@ __global__ void k_gram_reduce(const cplx_t<T>* __restrict__ partial, int splits,
 }
 
 struct GramPlan {
+  int shape;  // threads along i: 16 (64 x 64 tiles), 32 (128 x 32) or 8 (32 x 128)
   int ti, tj, splits, g_per_split;
   size_t partial_bytes;
 };
 static GramPlan gram_plan(int nk, int M, int N, int K, size_t elem) {
   GramPlan p;
-  p.ti = (M + GT - 1) / GT;
-  p.tj = (N + GT - 1) / GT;
+  p.shape = (N <= 32 && M > 32) ? 32 : ((M <= 32 && N > 32) ? 8 : 16);
+  const int bi = 4 * p.shape, bj = 4 * (256 / p.shape);
+  p.ti = (M + bi - 1) / bi;
+  p.tj = (N + bj - 1) / bj;
   const int tiles = p.ti * p.tj * nk;
   const int kchunks = (K + GK - 1) / GK;
   // Enough CTAs for two waves over the SMs, with at least 8 stages of g each.
@@ -300,6 +311,16 @@ size_t gram_workspace_bytes(int dtype, int nk, int M, int N, int K) {
   return gram_plan(nk, M, N, K, elem_bytes(dtype)).partial_bytes;
 }
 
+template <typename T, typename OutT>
+static void launch_gram(int shape, dim3 grid, const GramArgs& g, cudaStream_t st) {
+  if (shape == 32)
+    k_gram<T, OutT, 32><<<grid, 256, 0, st>>>(g);
+  else if (shape == 8)
+    k_gram<T, OutT, 8><<<grid, 256, 0, st>>>(g);
+  else
+    k_gram<T, OutT, 16><<<grid, 256, 0, st>>>(g);
+}
+
 // out(i, j) of type out_dtype (complex) = sum_g conj(A(i, g)) B(j, g), per k.
 int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, const void* B, long long b_batch,
          int ldb, int nk, int M, int N, int K, void* out, long long out_batch, int oi, int oj, void* ws,
@@ -318,11 +339,11 @@ int gram(int dtype, int out_dtype, const void* A, long long a_batch, int lda, co
              weight, real_out ? 1 : 0};
   const dim3 grid(p.ti, p.tj, nk * p.splits);
   if (dtype == QGB_F64) {
-    k_gram<double, double><<<grid, 256, 0, st>>>(g);
+    launch_gram<double, double>(p.shape, grid, g, st);
   } else if (out_dtype == QGB_F64) {
-    k_gram<float, double><<<grid, 256, 0, st>>>(g);
+    launch_gram<float, double>(p.shape, grid, g, st);
   } else {
-    k_gram<float, float><<<grid, 256, 0, st>>>(g);
+    launch_gram<float, float>(p.shape, grid, g, st);
   }
   QGB_LAUNCH_CHECK("k_gram");
   if (p.splits > 1) {

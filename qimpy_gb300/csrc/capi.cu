@@ -72,7 +72,12 @@ size_t nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot);
 int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
                 int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, cudaStream_t st);
 int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
-                      int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, int phases, cudaStream_t st);
+                      int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, int phases, cudaStream_t st,
+                      const double* weight = nullptr);
+int check_real_map(const qgb_real_map* m, const qgb_sphere* full);
+size_t real_local_bytes(const qgb_sphere& full, const qgb_real_map& m, int nb, int dtype);
+int real_local(const qgb_sphere* full, const qgb_real_map* m, int dtype, const void* C, void* HC, int nb, void* ws,
+               size_t ws_bytes, cudaStream_t st);
 
 // A side stream and a fork/join event pair per (host thread, device): the mixed
 // Hamiltonian runs the C-only part of its nonlocal term there, beside the local
@@ -312,5 +317,45 @@ int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, 
   return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl, dev_error, 2, st);
 }
 
+size_t qgb_hamiltonian_real_mixed_workspace_bytes(const qgb_sphere* full, const qgb_real_map* map, int nb, int P) {
+  if (!full || !map || nb < 0 || P < 0) return 0;
+  const size_t nl = P > 0 ? (nonlocal_tc_workspace_bytes(1, P, nb, map->n_tot_half) + 255) / 256 * 256 : 0;
+  return nl + real_local_bytes(*full, *map, nb, QGB_F32);
+}
+
+int qgb_hamiltonian_real_mixed(const qgb_sphere* full, const qgb_real_map* map, const void* C, void* HC, int nb,
+                               const void* beta_split, const void* D, int n_atoms, int pa, void* projT,
+                               void* workspace, size_t workspace_bytes, int* dev_error, void* stream) {
+  int rc = validate_sphere(full, QGB_F32);
+  if (rc) return rc;
+  if ((rc = check_real_map(map, full))) return rc;
+  if (nb < 0 || n_atoms < 0 || pa < 0) return fail(QGB_ERR_INVALID, "negative sizes");
+  if (nb == 0) return QGB_OK;
+  if (!C || !HC) return fail(QGB_ERR_INVALID, "NULL wavefunction pointer");
+  if (C == HC) return fail(QGB_ERR_INVALID, "C and HC must not alias");
+  const int P = n_atoms * pa;
+  const size_t nl = P > 0 ? (nonlocal_tc_workspace_bytes(1, P, nb, map->n_tot_half) + 255) / 256 * 256 : 0;
+  if (!workspace || workspace_bytes < nl + real_local_bytes(*full, *map, nb, QGB_F32))
+    return fail(QGB_ERR_WORKSPACE, "workspace %zu B < %zu B", workspace_bytes,
+                nl + real_local_bytes(*full, *map, nb, QGB_F32));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* ws = static_cast<char*>(workspace);
+  if (P == 0) return real_local(full, map, QGB_F32, C, HC, nb, ws, workspace_bytes, st);
+  SideStream f;
+  if ((rc = side_stream(&f))) return rc;
+  // As qgb_hamiltonian_mixed: the weighted real projection on the side stream
+  // beside the local potential, joined before the back-projection.
+  QGB_CUDA_CHECK(cudaEventRecord(f.fork, st));
+  QGB_CUDA_CHECK(cudaStreamWaitEvent(f.side, f.fork, 0));
+  const int rc_front = nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, 1, nb, map->n_tot_half, ws, nl,
+                                         dev_error, 1, f.side, map->weight);
+  QGB_CUDA_CHECK(cudaEventRecord(f.join, f.side));
+  rc = real_local(full, map, QGB_F32, C, HC, nb, ws + nl, workspace_bytes - nl, st);
+  QGB_CUDA_CHECK(cudaStreamWaitEvent(st, f.join, 0));
+  if (rc_front) return rc_front;
+  if (rc) return rc;
+  return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, 1, nb, map->n_tot_half, ws, nl, dev_error, 2,
+                           st, map->weight);
+}
 
 }  // extern "C"

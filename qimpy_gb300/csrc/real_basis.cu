@@ -129,7 +129,7 @@ __global__ void k_symmetrize_real(cplx_t<T>* __restrict__ X, int n_tot_half, con
 
 static inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
-static int check_map(const qgb_real_map* m, const qgb_sphere* full) {
+int check_map(const qgb_real_map* m, const qgb_sphere* full) {
   if (!m || !full) return fail(QGB_ERR_INVALID, "NULL real-basis map or sphere");
   if (m->n_half < 1 || m->n_tot_half < m->n_half || m->n_full < m->n_half || m->n_plane < 0 ||
       m->n_plane > m->n_half)
@@ -163,6 +163,8 @@ static RealLayout real_layout(const qgb_sphere& full, const qgb_real_map& m, int
 
 using namespace rb;
 
+int check_real_map(const qgb_real_map* m, const qgb_sphere* full) { return check_map(m, full); }
+
 static int real_pack(int dtype, const qgb_real_map* m, const void* C, int nb, void* Z, cudaStream_t st) {
   const int nz = (nb + 1) / 2;
   if (nz == 0) return QGB_OK;
@@ -194,6 +196,24 @@ static int real_unpack(int dtype, const qgb_real_map* m, const void* W, const vo
                                                     static_cast<float2*>(out));
   QGB_LAUNCH_CHECK("k_unpack_real");
   return QGB_OK;
+}
+
+// The local part alone (pack, full-sphere potential with the KE term, unpack):
+// workspace Z, W and the slab planes.
+size_t real_local_bytes(const qgb_sphere& full, const qgb_real_map& m, int nb, int dtype) {
+  const RealLayout L = real_layout(full, m, nb, 0, dtype);
+  return L.z + L.w + L.planes;
+}
+
+int real_local(const qgb_sphere* full, const qgb_real_map* m, int dtype, const void* C, void* HC, int nb, void* ws,
+               size_t ws_bytes, cudaStream_t st) {
+  const RealLayout L = real_layout(*full, *m, nb, 0, dtype);
+  if (ws_bytes < L.z + L.w + L.planes) return fail(QGB_ERR_WORKSPACE, "real local workspace too small");
+  char* w = static_cast<char*>(ws);
+  int rc;
+  if ((rc = real_pack(dtype, m, C, nb, w, st))) return rc;
+  if ((rc = apply_potential(full, dtype, w, w + L.z, (nb + 1) / 2, 0u, w + L.z + L.w, L.planes, st))) return rc;
+  return real_unpack(dtype, m, w + L.z, C, nb, HC, QGB_ADD_KE, st);
 }
 
 }  // namespace qgb

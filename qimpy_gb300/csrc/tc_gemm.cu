@@ -409,9 +409,12 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
 
 // Wavefunction rows for the B operand: complex64 C[k][nb][n_tot] -> rows
 // r = t*BN + part*HB + j (band t*HB + j, part 0 = real, 1 = imaginary) of
-// [k][rows][ld] bf16 hi/lo; bands >= nb give zero rows.
+// [k][rows][ld] bf16 hi/lo; bands >= nb give zero rows.  With `weight`
+// (real wavefunctions: 1 on the Gz = 0 plane, 2 elsewhere; powers of two, so
+// the split stays exact) every coefficient is scaled by w_g.
 __global__ void k_split_bands(const float2* __restrict__ C, int nb, int n_tot, int HB, int rows, int ld,
-                              __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+                              const double* __restrict__ weight, __nv_bfloat16* __restrict__ hi,
+                              __nv_bfloat16* __restrict__ lo) {
   const int r = blockIdx.y, k = blockIdx.z;
   const int t = r / (2 * HB), rem = r - t * 2 * HB, part = rem / HB, b = t * HB + rem % HB;
   const float2* src = C + (static_cast<long long>(k) * nb + b) * n_tot;
@@ -421,6 +424,7 @@ __global__ void k_split_bands(const float2* __restrict__ C, int nb, int n_tot, i
     if (b < nb && g < n_tot) {
       const float2 c = src[g];
       v = part ? c.y : c.x;
+      if (weight) v *= static_cast<float>(weight[g]);
     }
     __nv_bfloat16 h, l;
     split_bf16(v, h, l);
@@ -470,7 +474,7 @@ __global__ void k_split_beta(const float2* __restrict__ beta, int P, int n_tot, 
 // Block (32, 8): threadIdx.x runs along bands, threadIdx.y strides the splits;
 // the 8 partial sums of each band are combined in shared memory.
 __global__ void k_reduce_proj(const float* __restrict__ partial, int splits, long long part_rows, int part_ld,
-                              int P, int nb, int HB, float2* __restrict__ projT) {
+                              int P, int nb, int HB, int real_out, float2* __restrict__ projT) {
   __shared__ float2 acc[8][32];
   const int k = blockIdx.z, p = blockIdx.y;
   const int b = blockIdx.x * 32 + threadIdx.x;
@@ -495,6 +499,7 @@ __global__ void k_reduce_proj(const float* __restrict__ partial, int splits, lon
       sum.x += acc[y][threadIdx.x].x;
       sum.y += acc[y][threadIdx.x].y;
     }
+    if (real_out) sum.y = 0.f;  // real wavefunctions: the implicit -G partners cancel it
     projT[(static_cast<long long>(k) * nb + b) * P + p] = sum;
   }
 }
@@ -614,7 +619,7 @@ size_t nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot) {
 template <int BN>
 static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC,
                             void* projT, int nk, int nb, int n_tot, const NlWorkspace& W, unsigned char* ws,
-                            int* err, int phases, cudaStream_t st) {
+                            int* err, int phases, const double* weight, cudaStream_t st) {
   const int P = n_atoms * pa;
   const BetaSplitLayout BL = beta_layout(nk, P, n_tot);
   auto* sbase = reinterpret_cast<const __nv_bfloat16*>(round_up(reinterpret_cast<uintptr_t>(split), 256));
@@ -634,7 +639,7 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
   {
     dim3 grid(static_cast<unsigned>(std::min<long long>(32, (W.ldB + 255) / 256)), static_cast<unsigned>(W.rowsB), nk);
     k_split_bands<<<grid, 256, 0, st>>>(static_cast<const float2*>(C), nb, n_tot, W.HB, static_cast<int>(W.rowsB),
-                                        static_cast<int>(W.ldB), b_hi, b_lo);
+                                        static_cast<int>(W.ldB), weight, b_hi, b_lo);
     QGB_LAUNCH_CHECK("k_split_bands");
   }
   // 2. <beta|psi> partials: M = 2P, N = rowsB, K = basis, split-K.
@@ -656,7 +661,7 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
   {
     dim3 grid((nb + 31) / 32, P, nk);
     k_reduce_proj<<<grid, dim3(32, 8), 0, st>>>(partial, W.splits, g1.part_rows, g1.part_ld, P, nb, W.HB,
-                                                static_cast<float2*>(projT));
+                                                weight != nullptr, static_cast<float2*>(projT));
     QGB_LAUNCH_CHECK("k_reduce_proj");
     dim3 grid2(1, static_cast<unsigned>(W.rowsB), nk);
     k_dapply_split<<<grid2, 256, 0, st>>>(static_cast<const float2*>(projT), static_cast<const float2*>(D),
@@ -684,7 +689,8 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
 }
 
 int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
-                      int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, int phases, cudaStream_t st) {
+                      int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, int phases, cudaStream_t st,
+                      const double* weight) {
   const int P = n_atoms * pa;
   if (nk < 1 || nb < 0 || n_tot < 1 || P < 0) return fail(QGB_ERR_INVALID, "bad nonlocal_tc sizes");
   if (nb == 0 || P == 0) return QGB_OK;
@@ -695,17 +701,20 @@ int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, con
   unsigned char* w = static_cast<unsigned char*>(ws);
   switch (W.BN) {
     case 64:
-      return nonlocal_tc_impl<64>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, st);
+      return nonlocal_tc_impl<64>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, weight,
+                                  st);
     case 128:
-      return nonlocal_tc_impl<128>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, st);
+      return nonlocal_tc_impl<128>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, weight,
+                                   st);
     default:
-      return nonlocal_tc_impl<256>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, st);
+      return nonlocal_tc_impl<256>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, weight,
+                                   st);
   }
 }
 
 int nonlocal_tc(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC, void* projT,
                 int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, cudaStream_t st) {
-  return nonlocal_tc_phase(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, ws, ws_bytes, err, 3, st);
+  return nonlocal_tc_phase(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, ws, ws_bytes, err, 3, st, nullptr);
 }
 
 // Test aid for the bounded waits: one CTA of the GEMM whose producer issues

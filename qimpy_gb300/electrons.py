@@ -155,8 +155,7 @@ class Ions:
             self.n_projectors = int(beta.shape[1])
         # Mixed form: bf16 hi/lo projector operands for the tensor-core GEMMs.
         self.beta_split = (ops.beta_split(self.beta)
-                           if self.beta is not None and basis.dtype == torch.complex64 and basis.real is None
-                           else None)
+                           if self.beta is not None and basis.dtype == torch.complex64 else None)
         self.beta_version = 0
 
     def D_all(self) -> torch.Tensor:
@@ -305,7 +304,9 @@ class Electrons:
         """HC in one C-ABI call: fused KE + local potential, then the nonlocal
         term (FP64: ZGEMMs; mixed: tcgen05 split-BF16x3 GEMMs)."""
         ions = self.ions
-        if self.basis.real is not None:
+        if self.basis.real is not None and self.basis.dtype == torch.complex64:
+            HC, projT = ops.hamiltonian_real_mixed(self.basis.real, C.coeff, ions.beta_split, ions.D)
+        elif self.basis.real is not None:
             beta = ions.beta if ions.n_projectors else None
             HC, projT = ops.hamiltonian_real(self.basis.real, C.coeff, beta, ions.D)
         elif self.basis.dtype == torch.complex64:

@@ -412,6 +412,38 @@ def hamiltonian_real(rb, C: torch.Tensor, beta: torch.Tensor | None, D_blocks: t
     return out, projT
 
 
+def hamiltonian_real_mixed(rb, C: torch.Tensor, split: torch.Tensor | None, D_blocks: torch.Tensor | None,
+                           out: torch.Tensor | None = None, projT: torch.Tensor | None = None,
+                           ws: torch.Tensor | None = None):
+    """(HC, projT) of real wavefunctions in the mixed form (complex64): FP32
+    local potential, weighted real projection and back-projection as tcgen05
+    split-BF16x3 GEMMs on ``beta_split`` operands of the half-basis beta."""
+    nb = _check_real(rb, C)
+    if C.dtype != torch.complex64:
+        raise TypeError("the mixed real form is complex64")
+    out = torch.empty_like(C) if out is None else out
+    _check_real(rb, out, "out")
+    if split is None:
+        n_atoms, pa, P = 0, 0, 0
+        sptr = dptr = pptr = 0
+    else:
+        n_atoms, pa, _ = D_blocks.shape
+        P = n_atoms * pa
+        if D_blocks.dtype != torch.complex64 or not D_blocks.is_contiguous():
+            raise ValueError("D_blocks must be contiguous complex64 (n_atoms, pa, pa)")
+        projT = torch.empty((1, nb, P), dtype=C.dtype, device=C.device) if projT is None else projT
+        sptr, dptr, pptr = split.data_ptr(), D_blocks.data_ptr(), projT.data_ptr()
+    lib = _lib.lib()
+    if ws is None:
+        ws = workspace(lib.qgb_hamiltonian_real_mixed_workspace_bytes(ct.byref(rb.sphere.struct), ct.byref(rb.struct),
+                                                                      nb, P), C.device)
+    err = device_error_word(C.device)
+    _lib.check(lib.qgb_hamiltonian_real_mixed(ct.byref(rb.sphere.struct), ct.byref(rb.struct), C.data_ptr(),
+                                              out.data_ptr(), nb, sptr, dptr, n_atoms, pa, pptr, ws.data_ptr(),
+                                              ws.numel(), err.data_ptr(), _stream()), "hamiltonian_real_mixed")
+    return out, projT
+
+
 def dot_real(X: torch.Tensor, Y: torch.Tensor, weight: torch.Tensor, out: torch.Tensor | None = None):
     """out[0, i, j] = Re sum_g w_g conj(X[0, i, g]) Y[0, j, g] as complex128
     (imaginary part 0): the overlap of real wavefunctions on the half basis."""

@@ -75,6 +75,27 @@ def test_real_hamiltonian_matches_oracle(name, nb, hermitian, dtype):
     assert _rel(projT.cpu().numpy().astype(np.complex128).transpose(0, 2, 1), want_proj) <= TOL[dtype]
 
 
+@pytest.mark.parametrize("name,nb,hermitian", [("tiny_gamma", 5, False), ("si2", 7, True), ("si64", 32, True)])
+def test_real_hamiltonian_mixed_matches_oracle(name, nb, hermitian):
+    """Mixed form: FP32 local potential, weighted real projection and
+    back-projection on the tcgen05 split-BF16x3 GEMMs; within 2e-5 of the
+    oracle's FP64 H.psi, projections included."""
+    p, half, rb, beta = _setup(name, torch.complex64)
+    C = wl.make_wavefunctions(p, half, nb)
+    oh.constrain(C, half.n)
+    if hermitian:
+        oh.real_symmetrize(C, half.iG[0], p.grid_shape)
+    want, want_proj = _oracle(p, half, beta, C)
+    split = ops.beta_split(torch.from_numpy(beta).to(DEV, torch.complex64))
+    HC, projT = ops.hamiltonian_real_mixed(rb, torch.from_numpy(C).to(DEV, torch.complex64), split,
+                                           torch.from_numpy(p.D_atom).to(DEV, torch.complex64))
+    torch.cuda.synchronize()
+    assert int(ops.device_error_word(DEV).item()) == 0
+    assert _rel(HC.cpu().numpy().astype(np.complex128), want) <= TOL[torch.complex64]
+    pr = projT.cpu().numpy().astype(np.complex128).transpose(0, 2, 1)
+    assert _rel(pr, want_proj) <= TOL[torch.complex64] and not pr.imag.any()
+
+
 def test_real_hamiltonian_without_projectors_and_errors():
     p, half, rb, beta = _setup("tiny_gamma", torch.complex128)
     C = wl.make_wavefunctions(p, half, 3)
