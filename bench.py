@@ -268,7 +268,9 @@ NCU_DRAM_BYTES_PER_BLOCK = {"local": 295.0e6, "nonlocal": 195.9e6}
 # oracle port on the same inputs and host (si64, every host thread of an
 # 8-core x86 host: 1.7x at 2 bands, 1.9x at 8, 3.3x at 32); the reference
 # cannot run on the GPU host, so the CPU baseline there is the port.
-REFERENCE_OVER_PORT = {"2": 1.74, "8": 1.93, "32": 3.35, "host": "8-core x86 container, torch 2.11 CPU"}
+#: Reference H.psi time over the torch port's (oracle/hpsi_torch.py), si64 by
+#: band count, both on all 8 cores of one x86 host (tests/golden/time_reference_vs_port.py).
+REFERENCE_OVER_PORT = {"2": 0.78, "8": 1.03, "32": 1.09, "host": "8-core x86 container, torch 2.11 CPU"}
 
 
 def local_roofline(rc, band_apps, t_loc, hbm_peak, peaks) -> dict:
@@ -778,29 +780,34 @@ def run_serving(args, local):
 
 
 def cpu_baseline(args, p=None, b=None, beta=None, C=None, threads=None):
-    """Oracle H.psi (FP64, numpy/scipy) on a bounded band sample, timed on host cores."""
-    from oracle import hpsi as oh
+    """The reference's FP64 H.psi restated with torch CPU operations (the
+    reference's own library and steps: scatter, ifftn, *V, fftn, gather per
+    band; nonlocal as complex matmuls) on a bounded band sample, timed on every
+    host core.  The reference itself cannot travel to the GPU host; on one x86
+    host the port runs at the reference's speed (REFERENCE_OVER_PORT)."""
+    import torch
+
+    from oracle import hpsi_torch as oht
 
     threads = threads or os.cpu_count()
-    oh.set_threads(threads)
+    oht.set_threads(threads)
     if p is None:
         p, b, beta, C = make_workload(args.workload)
     nbs = max(1, args.cpu_sample_bands)
-    Cs = C[:, :nbs]
-    D = p.D_all()
-    Cs = np.ascontiguousarray(Cs)
-    oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, D, Cs)  # warm-up
+    Cs = np.ascontiguousarray(C[:, :nbs])
+    H = oht.Hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, p.D_all())
+    H(Cs)  # warm-up
     t0 = time.perf_counter()
     reps = 0
     while True:
-        oh.hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, D, Cs)
+        H(Cs)
         reps += 1
         if (time.perf_counter() - t0 > 10.0 and reps >= 3) or reps >= 20:
             break
     sec = (time.perf_counter() - t0) / reps
     return dict(value=nbs * p.nk / sec, unit=UNIT, cores=threads, kind="port",
                 sample=f"{nbs} bands x {p.nk} k of {args.workload} (one block), {reps} H.psi calls, "
-                       f"scipy.fft workers={threads}",
+                       f"torch {torch.__version__} CPU with {threads} threads",
                 reference_over_port_measured=REFERENCE_OVER_PORT)
 
 

@@ -5,7 +5,8 @@ baseline runs the oracle port (oracle.hpsi.hamiltonian, numpy/scipy).  This
 script measures, on one host, how fast the unmodified reference's
 Electrons.hamiltonian (torch CPU, every host thread) is relative to the port on
 the same inputs (every host thread), so that the baseline's ratio can be
-restated for the reference itself.  It needs the reference source (the
+restated for the reference itself; the torch port (oracle/hpsi_torch.py) is timed
+beside both.  It needs the reference source (the
 golden-vector recipe's import, single-rank stand-ins for mpi4py and friends).
 
     python tests/golden/time_reference_vs_port.py [--ref-src PATH] [--name si64] [--bands 2 8]
@@ -31,6 +32,7 @@ sys.path.insert(0, HERE)
 from make_golden import build_system, import_reference, inject  # noqa: E402
 
 from oracle import hpsi as oh  # noqa: E402
+from oracle import hpsi_torch as oht  # noqa: E402
 from qimpy_gb300 import workloads as wl  # noqa: E402
 
 
@@ -61,6 +63,7 @@ def main() -> None:
     el = inject(qimpy, system, prob, beta)
     threads = os.cpu_count()
     oh.set_threads(threads)
+    oht.set_threads(threads)
     D = prob.D_all()
     for nb in args.bands:
         C0 = wl.make_wavefunctions(prob, mine, nb)
@@ -72,11 +75,18 @@ def main() -> None:
         def port_call():
             return oh.hamiltonian(mine.ke, prob.V_r, mine.fft_index, mine.n, beta, D, C0)
 
+        H_torch = oht.Hamiltonian(mine.ke, prob.V_r, mine.fft_index, mine.n, beta, D)
+
+        def torch_port_call():
+            return H_torch(C0)
+
         t_ref = median_time(ref_call)
         t_port = median_time(port_call)
+        t_tport = median_time(torch_port_call)
         apps = nb * prob.nk
         print(json.dumps({"workload": args.name, "bands": nb, "threads": threads,
                           "reference_s": t_ref, "port_s": t_port,
+                          "torch_port_s": t_tport, "reference_over_torch_port": t_tport / t_ref,
                           "reference_band_apps_per_s": apps / t_ref, "port_band_apps_per_s": apps / t_port,
                           "reference_over_port": t_port / t_ref}), flush=True)
 

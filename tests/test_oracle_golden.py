@@ -219,3 +219,14 @@ def test_oracle_projectors_match_reference(name):
     assert np.abs(beta_b - ref).max() <= 1e-13 * np.abs(ref).max()
     assert np.abs(beta_g - wl.make_projectors(p, b)).max() <= 1e-14 * np.abs(ref).max()
     assert np.abs(beta_g - ref).max() <= 1e-8 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["tiny_fcc", "tiny_ortho"])
+def test_torch_port_matches_reference(name):
+    """The torch restatement used as the CPU baseline gives the reference's H.psi."""
+    from oracle import hpsi_torch as oht
+
+    g = _load(name)
+    p, b, beta, C = _problem(name, int(g["hpsi_bands"]))
+    HC = oht.Hamiltonian(b.ke, p.V_r, b.fft_index, b.n, beta, p.D_all())(C)
+    assert np.abs(HC - g["hpsi"]).max() <= 1e-12 * np.abs(g["hpsi"]).max()
