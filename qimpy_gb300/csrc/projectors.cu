@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads) k_projectors(const Params P, const i
       const double sg = P.sigma[s];
       double pw = sg * sg * sg;
       for (int e = 0; e < l; ++e) pw *= sg * sg;
-      R = 15.749609945653303 * pw * exp(-0.5 * sg * sg * q2);  // (2 pi)^{3/2} sigma^{2l+3}
+      R = 15.749609945722419 * pw * exp(-0.5 * sg * sg * q2);  // (2 pi)^{3/2} sigma^{2l+3}
       if (l & 1) R = -R;
     } else {
       R = blip_eval(P.coeff[s], P.n_coeff[s], P.dq[s], sqrt(q2));
