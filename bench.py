@@ -740,6 +740,7 @@ def run_batch(args, local):
                 sequential_value=bh.band_apps / float(np.median(seq)),
                 batched_over_sequential=float(np.median(seq)) / float(np.median(times)),
                 max_rel_diff_batched_vs_sequential=agree, launches_per_step=bh.launches(),
+                solo_instances=len(bh.solo), solo_units=bh.solo_units,
                 setup_s=t_setup, autotune_s=t_tune,
                 schedule={f"{k[0]}": [list(f) for f in v] for k, v in sched.items()},
                 error_word=int(ops.device_error_word(dev).item()))

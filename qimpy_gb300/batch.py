@@ -288,7 +288,9 @@ class BatchedHamiltonian:
     Instances are grouped by FFT grid shape; each group runs its local
     potential in three batched launches (shared memory sized for that shape)
     followed by the tensor-core nonlocal term of its instances.  Groups run on
-    separate streams, so a captured graph has one parallel branch per group."""
+    separate streams, so a captured graph has one parallel branch per group.
+    Instances large enough to fill the GPU alone (``solo_units``) run through
+    the single-instance call on a branch of their own."""
 
     instances: list
     device: torch.device
@@ -298,20 +300,37 @@ class BatchedHamiltonian:
     #: three transform phases); 0 = one chunk per group, the default: on the
     #: 256-instance batch 64 MB chunks measured 11% slower than one chunk.
     plane_chunk_bytes: int = 0
+    #: Instances with at least this many (k, band, slab) work units fill the GPU
+    #: by themselves (two waves of 152 SMs x 4 CTAs); they run through the
+    #: single-instance call (kernel parameters in constant memory, the
+    #: asynchronous x-pass without per-unit context staging) inside the same
+    #: graph, and only the smaller ones share batched launches.  0 batches all.
+    solo_units: int = 2 * 152 * 4
 
     def __post_init__(self):
         dev = self.device
         self.inputs = [inst.C for inst in self.instances]
         self.outputs = [torch.empty_like(inst.C) for inst in self.instances]
         by_shape: dict = {}
+        self.solo = []
         for i, inst in enumerate(self.instances):
-            by_shape.setdefault(inst.tables.shape, []).append(i)
+            t = inst.tables
+            if self.solo_units and t.nk * inst.nb * t.max_slabs >= self.solo_units:
+                self.solo.append(i)
+            else:
+                by_shape.setdefault(inst.tables.shape, []).append(i)
+        self._solo_ws = {i: ops.workspace(self.instances[i].sphere.hamiltonian_mixed_workspace_bytes(
+            self.instances[i].nb, self.instances[i].beta.shape[1]), dev) for i in self.solo}
+        self._solo_projT = {i: torch.empty((self.instances[i].nk, self.instances[i].nb,
+                                            self.instances[i].beta.shape[1]), dtype=torch.complex64, device=dev)
+                            for i in self.solo}
         # Largest groups first: their branches start earliest.
         order = sorted(by_shape.values(), key=lambda idx: -sum(self.instances[i].band_apps for i in idx))
         chunk = self.plane_chunk_bytes or (1 << 62)
         self.groups = [_Group([self.instances[i] for i in idx], [self.inputs[i] for i in idx],
                               [self.outputs[i] for i in idx], dev, chunk) for idx in order]
         self._streams = [torch.cuda.Stream(device=dev) for _ in self.groups]
+        self._solo_stream = torch.cuda.Stream(device=dev)
         self.graph = None
 
     @property
@@ -319,17 +338,25 @@ class BatchedHamiltonian:
         return sum(inst.band_apps for inst in self.instances)
 
     def launches(self) -> int:
-        """Kernels of ours per application: 3 batched local per chunk of a group + 5 per instance nonlocal."""
-        return 3 * sum(len(g._chunks) for g in self.groups) + 5 * len(self.instances)
+        """Kernels of ours per application: 3 batched local per chunk of a group,
+        3 local per solo instance, + 5 nonlocal per instance."""
+        return 3 * sum(len(g._chunks) for g in self.groups) + 3 * len(self.solo) + 5 * len(self.instances)
 
     def apply(self):
         """Out_i = H_i C_i for every instance (inputs/outputs fixed at construction)."""
         main = torch.cuda.current_stream()
+        if self.solo:
+            self._solo_stream.wait_stream(main)
+            with torch.cuda.stream(self._solo_stream):
+                for i in self.solo:
+                    inst = self.instances[i]
+                    ops.hamiltonian_mixed(inst.sphere, self.inputs[i], inst.split, inst.D, out=self.outputs[i],
+                                          projT=self._solo_projT[i], ws=self._solo_ws[i])
         for g, s in zip(self.groups, self._streams):
             s.wait_stream(main)
             with torch.cuda.stream(s):
                 g.apply()
-        for s in self._streams:
+        for s in self._streams + ([self._solo_stream] if self.solo else []):
             main.wait_stream(s)
 
     def capture(self):

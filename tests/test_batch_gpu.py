@@ -31,12 +31,17 @@ def _small_specs():
     return specs
 
 
-@pytest.mark.parametrize("chunk", [64 << 20, 1, 0])  # default, one instance per chunk, one chunk per group
-def test_batched_equals_individual_and_graph_replay(chunk):
+# plane chunks: 64 MB, one instance per chunk, one chunk per group; solo: none
+# batched alone, or the larger half of the instances through the single call
+@pytest.mark.parametrize("chunk,solo", [(64 << 20, False), (1, False), (0, False), (0, True)])
+def test_batched_equals_individual_and_graph_replay(chunk, solo):
     specs = _small_specs()
     insts = [bt.Instance(s, DEV) for s in specs]
     assert len({i.tables.shape for i in insts}) > 1  # uneven grids
-    bh = bt.BatchedHamiltonian(insts, torch.device(DEV), plane_chunk_bytes=chunk)
+    units = sorted(i.tables.nk * i.nb * i.tables.max_slabs for i in insts)
+    bh = bt.BatchedHamiltonian(insts, torch.device(DEV), plane_chunk_bytes=chunk,
+                               solo_units=units[len(units) // 2] if solo else 0)
+    assert (len(bh.solo) > 0) == solo and (not solo or len(bh.solo) < len(insts))
     if chunk == 1:
         assert sum(len(g._chunks) for g in bh.groups) == len(insts)
     bh.apply()
