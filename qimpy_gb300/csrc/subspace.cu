@@ -65,7 +65,18 @@ static int get_solver(Solver* out) {
   return QGB_OK;
 }
 
+// Few large matrices (the Gamma-only cells' expanded subspaces, n in the
+// hundreds) go through the divide-and-conquer syevd one matrix at a time; many
+// small ones through the batched syev.
+static bool per_matrix(int64_t nk, int64_t n) { return n >= 128 && nk <= 2; }
+
 static int query(const Solver& s, int64_t nk, int64_t n, size_t* dev_bytes, size_t* host_bytes) {
+  if (per_matrix(nk, n)) {
+    QGB_CUSOLVER(cusolverDnXsyevd_bufferSize(s.h, s.p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                             CUDA_C_64F, nullptr, n, CUDA_R_64F, nullptr, CUDA_C_64F, dev_bytes,
+                                             host_bytes));
+    return QGB_OK;
+  }
   QGB_CUSOLVER(cusolverDnXsyevBatched_bufferSize(s.h, s.p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
                                                  CUDA_C_64F, nullptr, n, CUDA_R_64F, nullptr, CUDA_C_64F,
                                                  dev_bytes, host_bytes, nk));
@@ -104,6 +115,13 @@ int qgb_subspace_eigh(void* A, double* W, int* info, int64_t nk, int64_t n, void
   static thread_local std::vector<unsigned char> host;
   if (host.size() < host_bytes + 1) host.resize(host_bytes + 1);
   QGB_CUSOLVER(cusolverDnSetStream(s.h, (cudaStream_t)stream));
+  if (per_matrix(nk, n)) {
+    for (int64_t k = 0; k < nk; ++k)
+      QGB_CUSOLVER(cusolverDnXsyevd(s.h, s.p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F,
+                                    static_cast<double2*>(A) + k * n * n, n, CUDA_R_64F, W + k * n, CUDA_C_64F,
+                                    workspace, dev_bytes, host.data(), host_bytes, info + k));
+    return QGB_OK;
+  }
   QGB_CUSOLVER(cusolverDnXsyevBatched(s.h, s.p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F, A,
                                       n, CUDA_R_64F, W, CUDA_C_64F, workspace, dev_bytes, host.data(), host_bytes,
                                       info, nk));
