@@ -330,7 +330,9 @@ class BatchedHamiltonian:
         self.groups = [_Group([self.instances[i] for i in idx], [self.inputs[i] for i in idx],
                               [self.outputs[i] for i in idx], dev, chunk) for idx in order]
         self._streams = [torch.cuda.Stream(device=dev) for _ in self.groups]
-        self._solo_stream = torch.cuda.Stream(device=dev)
+        # Solo instances spread over a few streams, so that the smaller of them
+        # overlap in the graph as the batched groups do.
+        self._solo_streams = [torch.cuda.Stream(device=dev) for _ in range(min(4, len(self.solo)))]
         self.graph = None
 
     @property
@@ -345,18 +347,18 @@ class BatchedHamiltonian:
     def apply(self):
         """Out_i = H_i C_i for every instance (inputs/outputs fixed at construction)."""
         main = torch.cuda.current_stream()
-        if self.solo:
-            self._solo_stream.wait_stream(main)
-            with torch.cuda.stream(self._solo_stream):
-                for i in self.solo:
-                    inst = self.instances[i]
-                    ops.hamiltonian_mixed(inst.sphere, self.inputs[i], inst.split, inst.D, out=self.outputs[i],
-                                          projT=self._solo_projT[i], ws=self._solo_ws[i])
+        for s in self._solo_streams:
+            s.wait_stream(main)
+        for j, i in enumerate(self.solo):
+            inst = self.instances[i]
+            with torch.cuda.stream(self._solo_streams[j % len(self._solo_streams)]):
+                ops.hamiltonian_mixed(inst.sphere, self.inputs[i], inst.split, inst.D, out=self.outputs[i],
+                                      projT=self._solo_projT[i], ws=self._solo_ws[i])
         for g, s in zip(self.groups, self._streams):
             s.wait_stream(main)
             with torch.cuda.stream(s):
                 g.apply()
-        for s in self._streams + ([self._solo_stream] if self.solo else []):
+        for s in self._streams + self._solo_streams:
             main.wait_stream(s)
 
     def capture(self):

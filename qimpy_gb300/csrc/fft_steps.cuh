@@ -286,13 +286,12 @@ __device__ __forceinline__ void run_pass_pairs(int R, const Pass ps) {
   }
 }
 
-// One pass of scalar (FP64) or paired (FP32) items.
+// One pass of the y/z transforms: scalar items (the paired form measured
+// slower there: two 8-byte accesses per element pair, separate twiddles per
+// lane and twice the registers).
 template <typename T, int S>
 __device__ __forceinline__ void run_pass_any(int R, const Pass ps) {
-  if constexpr (sizeof(T) == 4)
-    run_pass_pairs<S>(R, ps);
-  else
-    run_pass<T, S>(R, ps);
+  run_pass<T, S>(R, ps);
 }
 
 // Inverse transform (natural -> permuted) of nbatch pencils starting at shared

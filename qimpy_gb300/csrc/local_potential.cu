@@ -487,7 +487,7 @@ __device__ __forceinline__ void body_fft_yz_gather(const qgb_sphere& s, const Lo
 // ---------------------------------------------------------------------------
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_ifft_yz(const qgb_sphere s, LocalParams lp,
+__global__ void __launch_bounds__(kThreads) k_ifft_yz(const qgb_sphere s, LocalParams lp,
                                                       const cplx_t<T>* __restrict__ C,
                                                       cplx_t<T>* __restrict__ planes) {
   body_ifft_yz<T>(s, lp, C, planes, blockIdx.x, blockIdx.y, blockIdx.z);
@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(kThreads) k_xpass_async(const qgb_sphere s, Lo
 
 // C and out may alias (in-place apply): no __restrict__ on them.
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_fft_yz_gather(const qgb_sphere s, LocalParams lp,
+__global__ void __launch_bounds__(kThreads) k_fft_yz_gather(const qgb_sphere s, LocalParams lp,
                                                             const cplx_t<T>* C, cplx_t<T>* out,
                                                             const cplx_t<T>* __restrict__ planes) {
   body_fft_yz_gather<T>(s, lp, C, out, planes, blockIdx.x, blockIdx.y, blockIdx.z);
@@ -559,7 +559,7 @@ __device__ __forceinline__ long long batch_unit(BatchCtx& ctx, int& staged, cons
   }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_ifft_yz_batched(const qgb_batch_item* __restrict__ items,
+__global__ void __launch_bounds__(kThreads) k_ifft_yz_batched(const qgb_batch_item* __restrict__ items,
                                                               const int* __restrict__ unit_item,
                                                               const long long* __restrict__ starts,
                                                               long long n_units, int upc) {
@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(kThreads) k_xpass_batched(const qgb_batch_item
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_fft_yz_gather_batched(const qgb_batch_item* __restrict__ items,
+__global__ void __launch_bounds__(kThreads) k_fft_yz_gather_batched(const qgb_batch_item* __restrict__ items,
                                                                     const int* __restrict__ unit_item,
                                                                     const long long* __restrict__ starts,
                                                                     long long n_units, int upc) {

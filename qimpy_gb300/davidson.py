@@ -261,22 +261,128 @@ class Davidson:
 
 
 def refine_fp64(el_mixed: Electrons, el_fp64: Electrons, C: Optional[Wavefunction] = None,
-                eig_threshold: float = 1e-8, max_sweeps: int = 40, residual_threshold: Optional[float] = None):
+                eig_threshold: float = 1e-8, max_sweeps: int = 40, residual_threshold: Optional[float] = None,
+                method: str = "mixed_expansion", reset_every: int = 8):
     """FP64 refinement of mixed-precision eigenvectors.
 
-    Upcasts the vectors to complex128, orthonormalises them (Cholesky, FP64),
-    then runs FP64 Davidson sweeps (Rayleigh-Ritz with the FP64 Hamiltonian,
-    preconditioned residual expansion, expanded Rayleigh-Ritz) until the
-    eigenvalues change by less than `eig_threshold` (at most `max_sweeps`).
-    FP32 H.psi leaves eigenvalues with noise near eps_f32 * Ecut (~1e-6 Ha);
-    the FP64 sweeps remove it.  Returns (eigenvalues (nk, nb) FP64, refined FP64
-    Wavefunction); el_fp64 holds the refined state and `el_fp64.last_refine`
-    the sweep statistics.  With `residual_threshold` the sweeps also continue
-    until every band's FP64 residual norm is below it (at most `max_sweeps`)."""
+    Upcasts the vectors to complex128 and orthonormalises them (Cholesky,
+    FP64).  FP32 H.psi leaves eigenvalues with noise near eps_f32 * Ecut
+    (~1e-6 Ha); the sweeps below remove it.  Two methods:
+
+    * ``"fp64_sweeps"``: FP64 Davidson sweeps (the plain form's H.psi for the
+      current vectors and every expansion).
+    * ``"mixed_expansion"`` (default): FP64 H C once, then sweeps whose
+      expansion vectors (the FP64 preconditioned residuals) go through the
+      mixed H.psi only.  The Rayleigh-Ritz matrices are FP64: the coupling block
+      C^H H X is formed as (H C)^H X from the carried FP64 H C, so it is exact
+      to FP64; only the small expansion-expansion block X^H H X carries FP32
+      H.psi error (symmetrised), which perturbs the update at second order in
+      the residual.  H C is carried through the FP64 rotations; its error grows
+      by ~eps_f32 |H| times the size of each update, so a fresh FP64 H C replaces
+      it every `reset_every` sweeps and to confirm convergence (a Rayleigh-Ritz
+      with it, then the eigenvalue and residual tests).
+
+    Stops when the eigenvalues change by less than `eig_threshold` (and, with
+    `residual_threshold`, every requested band's FP64 residual norm is below
+    it), at most `max_sweeps` sweeps.  Returns (eigenvalues (nk, nb) FP64,
+    refined FP64 Wavefunction); el_fp64 holds the refined state and
+    `el_fp64.last_refine` the sweep statistics."""
     C = C or el_mixed.C
     C64 = Wavefunction(el_fp64.basis, coeff=C.coeff.to(torch.complex128))
     C64.constrain()
     el_fp64.C = C64.orthonormalize()
-    el_fp64.last_refine = Davidson(el_fp64, n_iterations=max_sweeps, eig_threshold=eig_threshold,
-                                   residual_threshold=residual_threshold)()
+    if method == "fp64_sweeps":
+        el_fp64.last_refine = Davidson(el_fp64, n_iterations=max_sweeps, eig_threshold=eig_threshold,
+                                       residual_threshold=residual_threshold)()
+    elif method == "mixed_expansion":
+        el_fp64.last_refine = _refine_mixed_expansion(el_mixed, el_fp64, eig_threshold, max_sweeps,
+                                                      residual_threshold, reset_every)
+    else:
+        raise ValueError(f"unknown refinement method {method!r}")
     return el_fp64.eig, el_fp64.C
+
+
+def _refine_mixed_expansion(el32: Electrons, el: Electrons, eig_threshold: float, max_sweeps: int,
+                            residual_threshold: Optional[float], reset_every: int) -> DavidsonStats:
+    basis = el.basis
+    real = basis.real is not None
+    w = basis.weight
+    cdt = torch.float64 if real else torch.complex128
+    n_bands = el.n_bands
+    n_bands_max = n_bands + el.n_bands_extra
+    norm_cut = float(np.sqrt(basis.n_tot * 1e-15))
+    if residual_threshold is not None:
+        norm_cut = min(norm_cut, 0.01 * residual_threshold)
+    hpsi64 = hpsi32 = 0
+
+    def fresh_rr():
+        """FP64 H C and a Rayleigh-Ritz rotation with it (eigenvalues to FP64)."""
+        nonlocal hpsi64
+        HC = el.hamiltonian(el.C)
+        hpsi64 += el.C.n_bands() * basis.nk
+        eig, V = eigh(_sub((el.C ^ HC).wait(), real))
+        el.C = el.C @ V
+        return eig, HC @ V
+
+    el.eig, HC = fresh_rr()
+    deig_max, res_max, converged = np.inf, np.inf, False
+    n_eigs_done = 0
+    sweeps = 0
+    since_reset = 0
+    while sweeps < max_sweeps:
+        sweeps += 1
+        since_reset += 1
+        n_cur = el.C.n_bands()
+        KEref = ops.band_norm_ke(el.C.coeff, basis.ke, b0=n_eigs_done, norm=False, weight=w)[1]
+        Cexp = Wavefunction(basis, coeff=torch.empty((basis.nk, n_cur - n_eigs_done, basis.n_tot),
+                                                     dtype=el.C.coeff.dtype, device=el.C.coeff.device))
+        norm_exp = ops.residual(HC.coeff, el.C.coeff, el.eig, basis.ke, KEref, b0=n_eigs_done, out=Cexp.coeff,
+                                norm=True, weight=w)
+        ops.normalize_bands(Cexp.coeff, basis.n_device, norm_exp, norm_cut, sweeps, basis.n_max, basis.ke)
+        if real:
+            ops.symmetrize_real(basis.real, Cexp.coeff)
+        # The expansion's H.psi in the mixed form, upcast.
+        HCexp32 = el32.hamiltonian(Wavefunction(el32.basis, coeff=Cexp.coeff.to(el32.basis.dtype)))
+        hpsi32 += Cexp.n_bands() * basis.nk
+        HCexp = Wavefunction(basis, coeff=HCexp32.coeff.to(torch.complex128))
+        n_exp = Cexp.n_bands()
+        Cnew = el.C.cat(Cexp)
+        O = _tile_expansion(torch.eye(n_cur, device=HC.coeff.device, dtype=cdt)[None], _sub((Cnew ^ Cexp).wait(), real))
+        coup = _sub((HC ^ Cexp).wait(), real)  # C^H H X = (H C)^H X, FP64
+        ee = _sub((Cexp ^ HCexp).wait(), real)
+        ee = 0.5 * (ee + ee.conj().transpose(-2, -1))
+        Hn = _tile_expansion(torch.diag_embed(el.eig).to(cdt), torch.cat((coup, ee), dim=1))
+        eig_new, V_new, failed = eighg(Hn, O, check=False)
+        n_next = min(n_cur + n_exp, n_bands_max)
+        d = torch.abs(el.eig - eig_new[..., :n_cur])[:, :n_bands]
+        pend = (d > eig_threshold).any(dim=0)
+        first_pending = torch.where(pend.any(), pend.int().argmax(), torch.tensor(n_bands, device=pend.device))
+        host = torch.stack((d.max(), first_pending.to(torch.float64), failed.any().to(torch.float64))).tolist()
+        if host[2]:
+            raise RuntimeError("refinement subspace problem failed: overlap not positive-definite")
+        V_new = V_new[..., :n_next]
+        Vcur, Vexp = V_new[:, :n_cur], V_new[:, n_cur:]
+        el.C = Cnew @ V_new
+        HC = HC @ Vcur
+        HC += HCexp @ Vexp
+        el.eig = eig_new[..., :n_next].contiguous()
+        deig_max = host[0]
+        n_eigs_done = int(host[1])
+        if n_eigs_done >= n_bands or since_reset >= reset_every:
+            # Fresh FP64 H C: Rayleigh-Ritz, then the convergence tests on it.
+            eig_prev = el.eig
+            el.eig, HC = fresh_rr()
+            since_reset = 0
+            d_rr = float(torch.abs(el.eig - eig_prev)[:, :n_bands].max())
+            if n_eigs_done >= n_bands:
+                converged = d_rr < eig_threshold
+                if converged and residual_threshold is not None:
+                    res = ops.residual(HC.coeff, el.C.coeff, el.eig, norm=True, weight=w)
+                    res_max = float(res[:, :n_bands].max())
+                    converged = res_max < residual_threshold
+                if converged:
+                    break
+                n_eigs_done = 0
+    el.deig_max = deig_max
+    return DavidsonStats(sweeps, converged, deig_max, res_max, hpsi32 + hpsi64, False)
+
