@@ -62,6 +62,8 @@ def parse_args():
     ap.add_argument("--serve", type=int, default=32, help="requests of the serving stream sample (0 = skip)")
     ap.add_argument("--serve-wall", type=float, default=150.0, help="wall-clock cap per serving run (s)")
     ap.add_argument("--no-eigensolve", action="store_true")
+    ap.add_argument("--profile-davidson", action="store_true",
+                    help="print torch.profiler kernel tables of Davidson solves (si2, si64) instead of the bench line")
     ap.add_argument("--autotune", action="store_true",
                     help="autotuned FFT factorisation for si64 (measured equal to the default within noise)")
     return ap.parse_args()
@@ -812,8 +814,45 @@ def cpu_baseline(args, p=None, b=None, beta=None, C=None, threads=None):
                 reference_over_port_measured=REFERENCE_OVER_PORT)
 
 
+def profile_davidson() -> None:
+    """Kernel time tables of Davidson solves (torch.profiler, CPU and CUDA
+    activities): si2 to convergence and si64 for 12 iterations, FP64 and
+    mixed; an unprofiled si2 solve of each form runs first as a warm-up."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+
+    from qimpy_gb300 import davidson as dv, electrons as E, workloads as wl
+
+    def solve(name, dtype, threshold, iters, prof):
+        p = wl.get(name)
+        el, C0 = E.from_problem(p, "cuda:0", dtype)
+        el.C = E.Wavefunction(el.basis, coeff=C0.to("cuda:0", dtype)).orthonormalize()
+        torch.cuda.synchronize()
+        d = dv.Davidson(el, n_iterations=iters, eig_threshold=threshold)
+        if not prof:
+            d()
+            return
+        with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as pr:
+            t0 = time.perf_counter()
+            st = d()
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        print(f"== {name} {dtype} iterations {st.iterations} wall {wall:.3f}s "
+              f"per-iteration {1e3 * wall / st.iterations:.2f} ms")
+        print(pr.key_averages().table(sort_by="cuda_time_total", row_limit=25, max_name_column_width=60))
+
+    for dt, thr in ((torch.complex128, 1e-11), (torch.complex64, 1e-6)):
+        solve("si2", dt, thr, 300, False)
+        solve("si2", dt, thr, 300, True)
+    for dt, thr in ((torch.complex128, 1e-9), (torch.complex64, 1e-6)):
+        solve("si64", dt, thr, 12, True)
+
+
 def main():
     args = parse_args()
+    if args.profile_davidson:
+        profile_davidson()
+        return
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:
