@@ -24,7 +24,6 @@
 // y/z passes and the empty z-rows in the z passes.
 #include <algorithm>
 #include <mutex>
-#include <type_traits>
 
 #include "fft_steps.cuh"
 
@@ -289,50 +288,6 @@ __device__ __forceinline__ void xmid_dispatch(int L1, cplx_t<T>* sm, int p, int 
   }
 }
 
-// The middle step on two adjacent columns (p, p + 1; FP32, p and ld even):
-// V pairs at Vp[j * vstride] (8-byte aligned), one twiddle per j shared by both.
-template <int R>
-__device__ __forceinline__ void xmid_item_x2(int p, int ld, const float* Vp, int vstride, int Wx, int L2, int a,
-                                             int lim) {
-  f32x2 re[R], im[R];
-  if (!load_x2<R>(p, ld, lim, re, im)) return;
-  Codelet<R, +1>::run(re, im);
-#pragma unroll
-  for (int j = 0; j < R; ++j) {
-    const f32x2 vv(*reinterpret_cast<const float2*>(Vp + j * vstride));
-    re[j] = re[j] * vv;
-    im[j] = im[j] * vv;
-  }
-  Codelet<R, -1>::run(re, im);
-  if (L2 > 1) {
-    const float2* sm = smem_c<float>();
-#pragma unroll
-    for (int j = 1; j < R; ++j) twiddle_x2<-1>(re[j], im[j], sm[Wx + j * L2 + a]);
-  }
-  store_x2<R>(p, ld, re, im);
-}
-
-__device__ __forceinline__ void xmid_dispatch_x2(int L1, int p, int ld, const float* Vp, int vstride, int Wx,
-                                                 int L2, int a, int lim) {
-  switch (L1) {
-    case 1: xmid_item_x2<1>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 2: xmid_item_x2<2>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 3: xmid_item_x2<3>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 4: xmid_item_x2<4>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 5: xmid_item_x2<5>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 6: xmid_item_x2<6>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 7: xmid_item_x2<7>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 8: xmid_item_x2<8>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 9: xmid_item_x2<9>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 10: xmid_item_x2<10>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 12: xmid_item_x2<12>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 14: xmid_item_x2<14>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 15: xmid_item_x2<15>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    case 16: xmid_item_x2<16>(p, ld, Vp, vstride, Wx, L2, a, lim); break;
-    default: break;
-  }
-}
-
 // x-pass with asynchronous staging (FP32, N2 % 4 == 0): the slab rows and the
 // CTA's V slice are copied to shared memory with cp.async (no register
 // staging); V streams in while the first inverse pass runs, so the middle
@@ -378,37 +333,20 @@ __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const Loca
   cp_async_wait<1>();
   __syncthreads();
 
-  if constexpr (std::is_same<T, float>::value) {
-    // All three steps take two adjacent columns per thread with the packed
-    // FP32 instructions (nz and ld are even: every column pair is 16-byte aligned).
-    if (L2 > 1) run_pass_x2<+1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
-    cp_async_wait<0>();
+  if (L2 > 1) {
+    run_pass<T, +1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int it = threadIdx.x; it < nz * L2; it += blockDim.x) {
+    const int a = it / nz;
+    const int c = it - a * nz;
+    xmid_dispatch<T>(L1, sm, c + a * L1 * ld, ld, Vs + a * L1 * nz + c, static_cast<size_t>(nz), Wx, L2, a);
+  }
+  __syncthreads();
+  if (L2 > 1) {
+    run_pass<T, -1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
     __syncthreads();
-    const int npairs = nz >> 1;
-    for (int it = threadIdx.x; it < npairs * L2; it += blockDim.x) {
-      const int a = it / npairs;
-      const int c = 2 * (it - a * npairs);
-      xmid_dispatch_x2(L1, c + a * L1 * ld, ld, Vs + a * L1 * nz + c, nz, Wx, L2, a, lim);
-    }
-    __syncthreads();
-    if (L2 > 1) {
-      run_pass_x2<-1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
-      __syncthreads();
-    }
-  } else {
-    if (L2 > 1) run_pass<T, +1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
-    cp_async_wait<0>();
-    __syncthreads();
-    for (int it = threadIdx.x; it < nz * L2; it += blockDim.x) {
-      const int a = it / nz;
-      const int c = it - a * nz;
-      xmid_dispatch<T>(L1, sm, c + a * L1 * ld, ld, Vs + a * L1 * nz + c, static_cast<size_t>(nz), Wx, L2, a);
-    }
-    __syncthreads();
-    if (L2 > 1) {
-      run_pass<T, -1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
-      __syncthreads();
-    }
   }
   for (int sl = warp; sl < nslabs; sl += nwarps) {
     C2* dst = base + sl * plane;
