@@ -226,6 +226,18 @@ size_t qgb_dot_workspace_bytes(int dtype, int nk, int nx, int ny, int n_tot);
 int qgb_dot(int dtype, const void* X, int nx, const void* Y, int ny, int nk, int n_tot, void* out,
             void* workspace, size_t workspace_bytes, void* stream);
 /*
+ * qgb_dot of complex64 X, Y on the tcgen05 tensor cores (mixed form: the
+ * subspace overlaps of Wavefunction.dot, qimpy/dft/electrons/_wavefunction_dot.py:18-107,
+ * as split-BF16x3 GEMMs with FP32 accumulation, the basis-range partial sums
+ * added in FP64): out complex128 [nk][nx][ny], about 16 significant bits per
+ * product.  Workspace of qgb_dot_tc_workspace_bytes; dev_error as for
+ * qgb_apply_nonlocal_tc.
+ */
+size_t qgb_dot_tc_workspace_bytes(int nk, int nx, int ny, int n_tot);
+int qgb_dot_tc(const void* X, int nx, const void* Y, int ny, int nk, int n_tot, void* out, void* workspace,
+               size_t workspace_bytes, int* dev_error, void* stream);
+
+/*
  * The overlap of real (Gamma-point) wavefunctions on the half basis:
  * out[i][j] = Re sum_g w_g conj(X[i][g]) Y[j][g] (imaginary part 0), weight
  * FP64 [n_tot], workspace of qgb_dot_workspace_bytes with nk = 1 (the

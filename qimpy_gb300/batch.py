@@ -166,7 +166,7 @@ class Instance:
         basis.fft_index, basis.iG, basis.tables, basis.sphere = self.layout.fft_index, self.layout.iG, \
             self.tables, self.sphere
         basis.ke = torch.from_numpy(self.layout.ke).to(self.sphere.device)
-        basis.real, basis.weight = None, None  # complex wavefunctions
+        basis.real, basis.weight, basis.tc_subspace = None, None, False  # complex wavefunctions
         pad = torch.arange(basis.n_tot)[None, :] < torch.from_numpy(basis.n)[:, None]
         basis.mask = pad.to(self.sphere.device)
         basis._V_id = id(self.V_r)

@@ -75,6 +75,9 @@ int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, con
                       int nk, int nb, int n_tot, void* ws, size_t ws_bytes, int* err, int phases, cudaStream_t st,
                       const double* weight = nullptr);
 int check_real_map(const qgb_real_map* m, const qgb_sphere* full);
+size_t gram_tc_workspace_bytes(int nk, int nx, int ny, int n);
+int gram_tc(const void* X, int nx, const void* Y, int ny, int nk, int n, double2* out, long long out_batch, int oi,
+            int oj, void* ws, size_t ws_bytes, int* err, cudaStream_t st);
 size_t real_local_bytes(const qgb_sphere& full, const qgb_real_map& m, int nb, int dtype);
 int real_local(const qgb_sphere* full, const qgb_real_map* m, int dtype, const void* C, void* HC, int nb, void* ws,
                size_t ws_bytes, cudaStream_t st);
@@ -180,6 +183,16 @@ int qgb_dot(int dtype, const void* X, int nx, const void* Y, int ny, int nk, int
   return gram(dtype, QGB_F64, X, static_cast<long long>(nx) * n_tot, n_tot, Y, static_cast<long long>(ny) * n_tot,
               n_tot, nk, nx, ny, n_tot, out, static_cast<long long>(nx) * ny, ny, 1, workspace, workspace_bytes,
               static_cast<cudaStream_t>(stream));
+}
+
+size_t qgb_dot_tc_workspace_bytes(int nk, int nx, int ny, int n_tot) {
+  return gram_tc_workspace_bytes(nk, nx, ny, n_tot);
+}
+
+int qgb_dot_tc(const void* X, int nx, const void* Y, int ny, int nk, int n_tot, void* out, void* workspace,
+               size_t workspace_bytes, int* dev_error, void* stream) {
+  return gram_tc(X, nx, Y, ny, nk, n_tot, static_cast<double2*>(out), static_cast<long long>(nx) * ny, ny, 1,
+                 workspace, workspace_bytes, dev_error, static_cast<cudaStream_t>(stream));
 }
 
 int qgb_dot_real(int dtype, const void* X, int nx, const void* Y, int ny, int n_tot, const double* weight, void* out,

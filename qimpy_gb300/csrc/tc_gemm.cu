@@ -436,7 +436,7 @@ __global__ void k_split_bands(const float2* __restrict__ C, int nb, int n_tot, i
 // Projector operands, once per basis: complex64 beta[k][P][n_tot] ->
 //   A  [k][2P][ldA]  rows (Re beta_p; Im beta_p), K = basis  (for <beta|psi>)
 //   AT [k][n_tot][ldT] row g = (Re beta_p(g), p < P; Im beta_p(g)), K = 2P
-//                                                     (for beta (D proj))
+//                                                     (for beta (D proj); skipped when t_hi is NULL)
 __global__ void k_split_beta(const float2* __restrict__ beta, int P, int n_tot, int ldA, int ldT,
                              __nv_bfloat16* __restrict__ a_hi, __nv_bfloat16* __restrict__ a_lo,
                              __nv_bfloat16* __restrict__ t_hi, __nv_bfloat16* __restrict__ t_lo) {
@@ -450,7 +450,7 @@ __global__ void k_split_beta(const float2* __restrict__ beta, int P, int n_tot, 
     split_bf16(c.x, h, l);
     a_hi[oa_r + g] = h;
     a_lo[oa_r + g] = l;
-    if (g < n_tot) {
+    if (t_hi != nullptr && g < n_tot) {
       const long long ot = (static_cast<long long>(k) * n_tot + g) * ldT;
       t_hi[ot + p] = h;
       t_lo[ot + p] = l;
@@ -458,7 +458,7 @@ __global__ void k_split_beta(const float2* __restrict__ beta, int P, int n_tot, 
     split_bf16(c.y, h, l);
     a_hi[oa_i + g] = h;
     a_lo[oa_i + g] = l;
-    if (g < n_tot) {
+    if (t_hi != nullptr && g < n_tot) {
       const long long ot = (static_cast<long long>(k) * n_tot + g) * ldT;
       t_hi[ot + P + p] = h;
       t_lo[ot + P + p] = l;
@@ -501,6 +501,29 @@ __global__ void k_reduce_proj(const float* __restrict__ partial, int splits, lon
     }
     if (real_out) sum.y = 0.f;  // real wavefunctions: the implicit -G partners cancel it
     projT[(static_cast<long long>(k) * nb + b) * P + p] = sum;
+  }
+}
+
+// Reduce split-K partials of a Gram product into out (complex128):
+// out[k*out_batch + i*oi + j*oj] = <X_i|Y_j>, partial rows i < nx Re X_i,
+// nx + i Im X_i; columns follow the band-row order of k_split_bands.  Splits
+// are summed in FP64, in split order.
+__global__ void k_reduce_gram(const float* __restrict__ partial, int splits, long long part_rows, int part_ld,
+                              int nx, int ny, int HB, double2* __restrict__ out, long long out_batch, int oi,
+                              int oj) {
+  const int k = blockIdx.z, i = blockIdx.y;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ny; j += gridDim.x * blockDim.x) {
+    const int t = j / HB, jj = j - t * HB;
+    const int c_re = t * 2 * HB + jj, c_im = c_re + HB;
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < splits; ++s) {
+      const float* D = partial + (static_cast<long long>(k) * splits + s) * part_rows * part_ld;
+      const float* r0 = D + static_cast<long long>(i) * part_ld;
+      const float* r1 = D + static_cast<long long>(nx + i) * part_ld;
+      re += static_cast<double>(r0[c_re]) + static_cast<double>(r1[c_im]);
+      im += static_cast<double>(r0[c_im]) - static_cast<double>(r1[c_re]);
+    }
+    out[k * out_batch + static_cast<long long>(i) * oi + static_cast<long long>(j) * oj] = make_double2(re, im);
   }
 }
 
@@ -709,6 +732,100 @@ int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, con
     default:
       return nonlocal_tc_impl<256>(split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, W, w, err, phases, weight,
                                    st);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Subspace Gram on the tensor cores (mixed form)
+// ---------------------------------------------------------------------------
+//
+// out[k][i][j] = sum_g conj(X[k][i][g]) Y[k][j][g] for complex64 X, Y: X split
+// as the A operand (rows Re X_i, Im X_i, K = basis), Y as band rows (B), the
+// split-K split-BF16x3 GEMM into FP32 partials, and the complex combination
+// summed over the splits in FP64.
+struct GramTcLayout {
+  long long ldA, a_elems, partial_floats, psi_elems, ldB, rowsB;
+  int splits, kb_per_split, HB, BN;
+};
+static GramTcLayout gram_tc_layout(int nk, int nx, int ny, int n) {
+  GramTcLayout G;
+  const NlWorkspace W = nl_layout(nk, nx, ny, n);  // the projection's layout with P -> nx
+  G.ldA = round_up(n, 64);
+  G.a_elems = static_cast<long long>(nk) * 2 * nx * G.ldA;
+  G.partial_floats = W.partial_floats;
+  G.psi_elems = W.psi_elems;
+  G.ldB = W.ldB;
+  G.rowsB = W.rowsB;
+  G.splits = W.splits;
+  G.kb_per_split = W.kb_per_split;
+  G.HB = W.HB;
+  G.BN = W.BN;
+  return G;
+}
+size_t gram_tc_workspace_bytes(int nk, int nx, int ny, int n) {
+  if (nk < 1 || nx < 1 || ny < 1 || n < 1) return 0;
+  const GramTcLayout G = gram_tc_layout(nk, nx, ny, n);
+  return static_cast<size_t>(round_up(G.partial_floats * 4, 256) + round_up(2 * G.a_elems * 2, 256) +
+                             round_up(2 * G.psi_elems * 2, 256)) + 1024;
+}
+
+template <int BN>
+static int gram_tc_impl(const GramTcLayout& G, const void* X, int nx, const void* Y, int ny, int nk, int n,
+                        double2* out, long long out_batch, int oi, int oj, unsigned char* ws, int* err,
+                        cudaStream_t st) {
+  unsigned char* p = reinterpret_cast<unsigned char*>(round_up(reinterpret_cast<uintptr_t>(ws), 256));
+  float* partial = reinterpret_cast<float*>(p);
+  p += round_up(G.partial_floats * 4, 256);
+  auto* a_hi = reinterpret_cast<__nv_bfloat16*>(p);
+  auto* a_lo = a_hi + G.a_elems;
+  p += round_up(2 * G.a_elems * 2, 256);
+  auto* b_hi = reinterpret_cast<__nv_bfloat16*>(p);
+  auto* b_lo = b_hi + G.psi_elems;
+  {
+    dim3 grid(static_cast<unsigned>(std::min<long long>(64, (G.ldA + 255) / 256)), nx, nk);
+    k_split_beta<<<grid, 256, 0, st>>>(static_cast<const float2*>(X), nx, n, static_cast<int>(G.ldA), 0, a_hi,
+                                       a_lo, nullptr, nullptr);
+    QGB_LAUNCH_CHECK("k_split_beta");
+    dim3 grid2(static_cast<unsigned>(std::min<long long>(32, (G.ldB + 255) / 256)), static_cast<unsigned>(G.rowsB),
+               nk);
+    k_split_bands<<<grid2, 256, 0, st>>>(static_cast<const float2*>(Y), ny, n, G.HB, static_cast<int>(G.rowsB),
+                                         static_cast<int>(G.ldB), nullptr, b_hi, b_lo);
+    QGB_LAUNCH_CHECK("k_split_bands");
+  }
+  GemmArgs g{};
+  g.M = 2 * nx;
+  g.N = static_cast<int>(G.rowsB);
+  g.K = n;
+  g.kb_per_split = G.kb_per_split;
+  g.splits = G.splits;
+  g.partial = partial;
+  g.part_ld = static_cast<int>(G.rowsB);
+  g.part_rows = (2LL * nx + BM - 1) / BM * BM;
+  g.err = err;
+  const int rc = launch<BN, kStages<BN>, EPI_PARTIAL>(
+      Operand{a_hi, a_lo, 2LL * nx, G.ldA, 2LL * nx * G.ldA}, Operand{b_hi, b_lo, G.rowsB, G.ldB, G.rowsB * G.ldB},
+      n, nk, g, st);
+  if (rc) return rc;
+  dim3 grid3(static_cast<unsigned>((ny + 127) / 128), nx, nk);
+  k_reduce_gram<<<grid3, 128, 0, st>>>(partial, G.splits, g.part_rows, g.part_ld, nx, ny, G.HB, out, out_batch, oi,
+                                       oj);
+  QGB_LAUNCH_CHECK("k_reduce_gram");
+  return QGB_OK;
+}
+
+int gram_tc(const void* X, int nx, const void* Y, int ny, int nk, int n, double2* out, long long out_batch, int oi,
+            int oj, void* ws, size_t ws_bytes, int* err, cudaStream_t st) {
+  if (nk < 0 || nx < 0 || ny < 0 || n < 1) return fail(QGB_ERR_INVALID, "bad gram_tc sizes");
+  if (nk == 0 || nx == 0 || ny == 0) return QGB_OK;
+  if (nk > 65535 || nx > 65535) return fail(QGB_ERR_UNSUPPORTED, "gram_tc: nk or nx above 65535");
+  if (!X || !Y || !out || !ws || !err) return fail(QGB_ERR_INVALID, "NULL pointer in gram_tc");
+  if (ws_bytes < gram_tc_workspace_bytes(nk, nx, ny, n)) return fail(QGB_ERR_WORKSPACE, "gram_tc workspace too small");
+  const GramTcLayout G = gram_tc_layout(nk, nx, ny, n);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  switch (G.BN) {
+    case 64: return gram_tc_impl<64>(G, X, nx, Y, ny, nk, n, out, out_batch, oi, oj, w, err, st);
+    case 128: return gram_tc_impl<128>(G, X, nx, Y, ny, nk, n, out, out_batch, oi, oj, w, err, st);
+    default: return gram_tc_impl<256>(G, X, nx, Y, ny, nk, n, out, out_batch, oi, oj, w, err, st);
   }
 }
 

@@ -58,6 +58,9 @@ class Basis:
         self.grid_shape = tuple(int(x) for x in grid_shape)
         self.device = torch.device(device)
         self.dtype = dtype
+        #: Mixed form: subspace overlaps of complex64 vectors on the tensor cores
+        #: (split-BF16x3, qgb_dot_tc) instead of the FP32 CUDA-core Gram.
+        self.tc_subspace = False
         self.real = None  #: DeviceRealBasis of the real-wavefunction mode
         self.weight = None  #: FP64 overlap weights of the half basis (real mode)
         if real:
@@ -210,7 +213,8 @@ class Wavefunction:
         and imaginary part zero (qgb_dot_real)."""
         if self.basis.real is not None:
             return Waitless(ops.dot_real(self.coeff, other.coeff, self.basis.weight))
-        return Waitless(ops.dot(self.coeff, other.coeff))
+        tc = self.basis.tc_subspace and self.coeff.dtype == torch.complex64
+        return Waitless(ops.dot(self.coeff, other.coeff, tc=tc))
 
     __xor__ = dot
     dot_O = dot

@@ -125,9 +125,10 @@ def _check_block(X: torch.Tensor, name: str) -> None:
     _qdtype(X)
 
 
-def dot(X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+def dot(X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None, tc: bool = False) -> torch.Tensor:
     """out[k, i, j] = sum_g conj(X[k, i, g]) Y[k, j, g] as complex128 (both
-    precisions; FP32 inputs are summed in FP32 per basis range, the ranges in FP64)."""
+    precisions; FP32 inputs are summed in FP32 per basis range, the ranges in FP64).
+    tc=True (complex64 only): on the tensor cores as split-BF16x3 GEMMs (qgb_dot_tc)."""
     _check_block(X, "X")
     _check_block(Y, "Y")
     if X.dtype != Y.dtype or X.shape[0] != Y.shape[0] or X.shape[2] != Y.shape[2] or X.device != Y.device:
@@ -142,6 +143,13 @@ def dot(X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None) -> to
         return out
     lib = _lib.lib()
     qd = _qdtype(X)
+    if tc:
+        if qd != _lib.QGB_F32:
+            raise TypeError("the tensor-core overlap takes complex64 vectors")
+        ws = workspace(lib.qgb_dot_tc_workspace_bytes(nk, nx, ny, n_tot), X.device)
+        _lib.check(lib.qgb_dot_tc(X.data_ptr(), nx, Y.data_ptr(), ny, nk, n_tot, out.data_ptr(), ws.data_ptr(),
+                                  ws.numel(), device_error_word(X.device).data_ptr(), _stream()), "dot_tc")
+        return out
     ws = workspace(lib.qgb_dot_workspace_bytes(qd, nk, nx, ny, n_tot), X.device)
     _lib.check(lib.qgb_dot(qd, X.data_ptr(), nx, Y.data_ptr(), ny, nk, n_tot, out.data_ptr(), ws.data_ptr(),
                            ws.numel(), _stream()), "dot")

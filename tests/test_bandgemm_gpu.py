@@ -38,6 +38,20 @@ def test_dot_matches_numpy(dtype, tol, nk, nx, ny, n):
     assert _err(got, want) < tol
 
 
+@pytest.mark.parametrize("nk,nx,ny,n", [(1, 7, 5, 33), (2, 65, 130, 1000), (1, 352, 176, 37073), (8, 36, 18, 1152)])
+def test_dot_tensor_cores_match_numpy(nk, nx, ny, n):
+    """qgb_dot_tc (split-BF16x3 on tcgen05, FP32 accumulation, FP64 split sums):
+    within 5e-5 of the FP64 product (max-norm relative)."""
+    X = _rand((nk, nx, n), 5, torch.complex64)
+    Y = _rand((nk, ny, n), 6, torch.complex64)
+    got = ops.dot(torch.from_numpy(X).to(DEV), torch.from_numpy(Y).to(DEV), tc=True).cpu().numpy()
+    torch.cuda.synchronize()
+    assert int(ops.device_error_word(DEV).item()) == 0
+    want = np.einsum("kig,kjg->kij", X.astype(np.complex128).conj(), Y.astype(np.complex128))
+    assert got.dtype == np.complex128
+    assert _err(got, want) < 5e-5
+
+
 @pytest.mark.parametrize("dtype,tol", [(torch.complex128, 1e-13), (torch.complex64, 5e-6)])
 @pytest.mark.parametrize("nk,n_in,n_out,n", [(1, 7, 5, 33), (2, 130, 65, 1001), (1, 352, 176, 37073)])
 def test_matmul_matches_numpy(dtype, tol, nk, n_in, n_out, n):
