@@ -238,6 +238,17 @@ int qgb_dot_tc(const void* X, int nx, const void* Y, int ny, int nk, int n_tot, 
                size_t workspace_bytes, int* dev_error, void* stream);
 
 /*
+ * qgb_matmul of complex64 C and M on the tcgen05 tensor cores (mixed form:
+ * Wavefunction.matmul, qimpy/dft/electrons/_wavefunction_dot.py:137-191, as
+ * one split-BF16x3 GEMM with FP32 accumulation into out): out complex64
+ * [nk][n_out][n_tot] (+= with QGB_ACCUMULATE), M complex64 [nk][n_in][n_out];
+ * out must not alias C.  Workspace of qgb_matmul_tc_workspace_bytes.
+ */
+size_t qgb_matmul_tc_workspace_bytes(int nk, int n_in, int n_out, int n_tot);
+int qgb_matmul_tc(const void* C, int n_in, int nk, int n_tot, const void* M, int n_out, void* out, unsigned flags,
+                  void* workspace, size_t workspace_bytes, int* dev_error, void* stream);
+
+/*
  * The overlap of real (Gamma-point) wavefunctions on the half basis:
  * out[i][j] = Re sum_g w_g conj(X[i][g]) Y[j][g] (imaginary part 0), weight
  * FP64 [n_tot], workspace of qgb_dot_workspace_bytes with nk = 1 (the

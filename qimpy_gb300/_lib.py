@@ -88,6 +88,9 @@ _SIGS = {
                                 ct.c_void_p]),
     "qgb_normalize_bands": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
                                        ct.c_double, ct.c_longlong, ct.c_longlong, ct.c_void_p, ct.c_void_p]),
+    "qgb_matmul_tc_workspace_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int, ct.c_int]),
+    "qgb_matmul_tc": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p,
+                                 ct.c_uint, ct.c_void_p, ct.c_size_t, ct.c_void_p, ct.c_void_p]),
     "qgb_dot_tc_workspace_bytes": (ct.c_size_t, [ct.c_int, ct.c_int, ct.c_int, ct.c_int]),
     "qgb_dot_tc": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p,
                               ct.c_void_p, ct.c_size_t, ct.c_void_p, ct.c_void_p]),

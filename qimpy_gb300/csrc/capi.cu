@@ -76,6 +76,9 @@ int nonlocal_tc_phase(const void* split, const void* D, int n_atoms, int pa, con
                       const double* weight = nullptr);
 int check_real_map(const qgb_real_map* m, const qgb_sphere* full);
 size_t gram_tc_workspace_bytes(int nk, int nx, int ny, int n);
+size_t rotate_tc_workspace_bytes(int nk, int n_in, int n_out, int n);
+int rotate_tc(const void* C, int n_in, int nk, int n, const void* M, int n_out, void* out, bool accumulate,
+              void* ws, size_t ws_bytes, int* err, cudaStream_t st);
 int gram_tc(const void* X, int nx, const void* Y, int ny, int nk, int n, double2* out, long long out_batch, int oi,
             int oj, void* ws, size_t ws_bytes, int* err, cudaStream_t st);
 size_t real_local_bytes(const qgb_sphere& full, const qgb_real_map& m, int nb, int dtype);
@@ -183,6 +186,17 @@ int qgb_dot(int dtype, const void* X, int nx, const void* Y, int ny, int nk, int
   return gram(dtype, QGB_F64, X, static_cast<long long>(nx) * n_tot, n_tot, Y, static_cast<long long>(ny) * n_tot,
               n_tot, nk, nx, ny, n_tot, out, static_cast<long long>(nx) * ny, ny, 1, workspace, workspace_bytes,
               static_cast<cudaStream_t>(stream));
+}
+
+size_t qgb_matmul_tc_workspace_bytes(int nk, int n_in, int n_out, int n_tot) {
+  return rotate_tc_workspace_bytes(nk, n_in, n_out, n_tot);
+}
+
+int qgb_matmul_tc(const void* C, int n_in, int nk, int n_tot, const void* M, int n_out, void* out, unsigned flags,
+                  void* workspace, size_t workspace_bytes, int* dev_error, void* stream) {
+  if (flags & ~QGB_ACCUMULATE) return fail(QGB_ERR_INVALID, "unknown matmul flags 0x%x", flags);
+  return rotate_tc(C, n_in, nk, n_tot, M, n_out, out, (flags & QGB_ACCUMULATE) != 0, workspace, workspace_bytes,
+                   dev_error, static_cast<cudaStream_t>(stream));
 }
 
 size_t qgb_dot_tc_workspace_bytes(int nk, int nx, int ny, int n_tot) {

@@ -565,6 +565,58 @@ __global__ void k_dapply_split(const float2* __restrict__ projT, const float2* _
   }
 }
 
+// Band rotation operands.  C complex64 [k][n_in][n] -> A [k][n][ldA]: row g =
+// (Re C_i(g), i < n_in; Im C_i(g)), K = 2 n_in, through a 32 x 32 shared tile
+// (coalesced reads along g, coalesced writes along i).
+__global__ void k_split_transpose(const float2* __restrict__ C, int n_in, int n, int ldA,
+                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+  __shared__ float2 tile[32][33];
+  const int k = blockIdx.z;
+  const int g0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, g = g0 + tx;
+    tile[r][tx] = (i < n_in && g < n) ? C[(static_cast<long long>(k) * n_in + i) * n + g] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int g = g0 + r, i = i0 + tx;
+    if (g >= n || i >= n_in) continue;
+    const float2 v = tile[tx][r];
+    const long long o = (static_cast<long long>(k) * n + g) * ldA;
+    __nv_bfloat16 h, l;
+    split_bf16(v.x, h, l);
+    hi[o + i] = h;
+    lo[o + i] = l;
+    split_bf16(v.y, h, l);
+    hi[o + n_in + i] = h;
+    lo[o + n_in + i] = l;
+  }
+}
+
+// Rotation matrix rows for the B operand: M complex64 [k][n_in][n_out] ->
+// rows r = t*BN + part*HB + jj (output band j = t*HB + jj) of [k][rows][ld],
+// K = 2 n_in: real-output rows (Re M_ij, -Im M_ij), imaginary-output rows
+// (Im M_ij, Re M_ij); bands >= n_out and the K padding are zero.
+__global__ void k_split_matrix(const float2* __restrict__ M, int n_in, int n_out, int HB, int rows, int ld,
+                               __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+  const int r = blockIdx.y, k = blockIdx.z;
+  const int t = r / (2 * HB), rem = r - t * 2 * HB, part = rem / HB, j = t * HB + rem % HB;
+  const long long o = (static_cast<long long>(k) * rows + r) * ld;
+  for (int p = threadIdx.x; p < ld; p += blockDim.x) {
+    float v = 0.f;
+    if (j < n_out && p < 2 * n_in) {
+      const int i = p < n_in ? p : p - n_in;
+      const float2 m = M[(static_cast<long long>(k) * n_in + i) * n_out + j];
+      v = p < n_in ? (part ? m.y : m.x) : (part ? m.x : -m.y);
+    }
+    __nv_bfloat16 h, l;
+    split_bf16(v, h, l);
+    hi[o + p] = h;
+    lo[o + p] = l;
+  }
+}
+
 static inline long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
 
 }  // namespace tc
@@ -826,6 +878,95 @@ int gram_tc(const void* X, int nx, const void* Y, int ny, int nk, int n, double2
     case 64: return gram_tc_impl<64>(G, X, nx, Y, ny, nk, n, out, out_batch, oi, oj, w, err, st);
     case 128: return gram_tc_impl<128>(G, X, nx, Y, ny, nk, n, out, out_batch, oi, oj, w, err, st);
     default: return gram_tc_impl<256>(G, X, nx, Y, ny, nk, n, out, out_batch, oi, oj, w, err, st);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Band rotation on the tensor cores (mixed form)
+// ---------------------------------------------------------------------------
+//
+// out[k][j][g] (+)= sum_i M[k][i][j] C[k][i][g] for complex64 C, M, out: C
+// transposed and split as the A operand (rows g, K = 2 n_in), M as rotation
+// rows (B), one split-BF16x3 GEMM accumulating into out in its epilogue.
+struct RotTcLayout {
+  long long ldA, a_elems, ldB, rowsB, b_elems;
+  int HB, BN;
+};
+static RotTcLayout rot_tc_layout(int nk, int n_in, int n_out, int n) {
+  RotTcLayout R;
+  R.BN = pick_bn(n_out);
+  R.HB = R.BN / 2;
+  R.rowsB = (n_out + R.HB - 1) / R.HB * static_cast<long long>(R.BN);
+  R.ldA = round_up(2LL * n_in, 64);
+  R.ldB = R.ldA;
+  R.a_elems = static_cast<long long>(nk) * n * R.ldA;
+  R.b_elems = static_cast<long long>(nk) * R.rowsB * R.ldB;
+  return R;
+}
+size_t rotate_tc_workspace_bytes(int nk, int n_in, int n_out, int n) {
+  if (nk < 1 || n_in < 1 || n_out < 1 || n < 1) return 0;
+  const RotTcLayout R = rot_tc_layout(nk, n_in, n_out, n);
+  return static_cast<size_t>(round_up(2 * R.a_elems * 2, 256) + round_up(2 * R.b_elems * 2, 256)) + 1024;
+}
+
+template <int BN>
+static int rotate_tc_impl(const RotTcLayout& R, const void* C, int n_in, int nk, int n, const void* M, int n_out,
+                          void* out, bool accumulate, unsigned char* ws, int* err, cudaStream_t st) {
+  unsigned char* p = reinterpret_cast<unsigned char*>(round_up(reinterpret_cast<uintptr_t>(ws), 256));
+  auto* a_hi = reinterpret_cast<__nv_bfloat16*>(p);
+  auto* a_lo = a_hi + R.a_elems;
+  p += round_up(2 * R.a_elems * 2, 256);
+  auto* b_hi = reinterpret_cast<__nv_bfloat16*>(p);
+  auto* b_lo = b_hi + R.b_elems;
+  // The K padding [2 n_in, ldA) of A is outside the tensor map's K extent and
+  // reads as zero; the transpose writes only the valid columns.
+  {
+    dim3 grid(static_cast<unsigned>((n + 31) / 32), static_cast<unsigned>((n_in + 31) / 32), nk);
+    k_split_transpose<<<grid, dim3(32, 8), 0, st>>>(static_cast<const float2*>(C), n_in, n, static_cast<int>(R.ldA),
+                                                  a_hi, a_lo);
+    QGB_LAUNCH_CHECK("k_split_transpose");
+    dim3 grid2(1, static_cast<unsigned>(R.rowsB), nk);
+    k_split_matrix<<<grid2, 256, 0, st>>>(static_cast<const float2*>(M), n_in, n_out, R.HB,
+                                          static_cast<int>(R.rowsB), static_cast<int>(R.ldB), b_hi, b_lo);
+    QGB_LAUNCH_CHECK("k_split_matrix");
+  }
+  if (!accumulate)
+    QGB_CUDA_CHECK(cudaMemsetAsync(out, 0, static_cast<size_t>(nk) * n_out * n * sizeof(float2), st));
+  GemmArgs g{};
+  g.M = n;
+  g.N = static_cast<int>(R.rowsB);
+  g.K = 2 * n_in;
+  g.kb_per_split = static_cast<int>((2LL * n_in + BK - 1) / BK);
+  g.splits = 1;
+  g.hc = static_cast<float2*>(out);
+  g.hc_batch_stride = static_cast<long long>(n_out) * n;
+  g.hc_ld = n;
+  g.nb = n_out;
+  g.err = err;
+  return launch<BN, kStages<BN>, EPI_ADD_HC>(Operand{a_hi, a_lo, n, R.ldA, static_cast<long long>(n) * R.ldA},
+                                             Operand{b_hi, b_lo, R.rowsB, R.ldB, R.rowsB * R.ldB}, 2 * n_in, nk, g,
+                                             st);
+}
+
+int rotate_tc(const void* C, int n_in, int nk, int n, const void* M, int n_out, void* out, bool accumulate,
+              void* ws, size_t ws_bytes, int* err, cudaStream_t st) {
+  if (nk < 0 || n_in < 0 || n_out < 0 || n < 1) return fail(QGB_ERR_INVALID, "bad rotate_tc sizes");
+  if (nk == 0 || n_out == 0) return QGB_OK;
+  if (n_in == 0) {
+    if (!accumulate) QGB_CUDA_CHECK(cudaMemsetAsync(out, 0, static_cast<size_t>(nk) * n_out * n * 8, st));
+    return QGB_OK;
+  }
+  if (nk > 65535) return fail(QGB_ERR_UNSUPPORTED, "rotate_tc: nk above 65535");
+  if (!C || !M || !out || !ws || !err) return fail(QGB_ERR_INVALID, "NULL pointer in rotate_tc");
+  if (C == out) return fail(QGB_ERR_INVALID, "C and out must not alias");
+  if (ws_bytes < rotate_tc_workspace_bytes(nk, n_in, n_out, n))
+    return fail(QGB_ERR_WORKSPACE, "rotate_tc workspace too small");
+  const RotTcLayout R = rot_tc_layout(nk, n_in, n_out, n);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  switch (R.BN) {
+    case 64: return rotate_tc_impl<64>(R, C, n_in, nk, n, M, n_out, out, accumulate, w, err, st);
+    case 128: return rotate_tc_impl<128>(R, C, n_in, nk, n, M, n_out, out, accumulate, w, err, st);
+    default: return rotate_tc_impl<256>(R, C, n_in, nk, n, M, n_out, out, accumulate, w, err, st);
   }
 }
 

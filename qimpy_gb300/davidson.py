@@ -191,7 +191,8 @@ class Davidson:
                 # new directions are a small part of Cexp, and keeping the rest
                 # would leave the overlap too ill-conditioned for FP32.
                 for _ in range(2):
-                    ops.matmul(el.C.coeff, -_sub((el.C ^ Cexp).wait(), real), out=Cexp.coeff, accumulate=True)
+                    ops.matmul(el.C.coeff, -_sub((el.C ^ Cexp).wait(), real), out=Cexp.coeff, accumulate=True,
+                               tc=basis.tc_subspace and not real)
                 norm_exp = Cexp.band_norm()
             ops.normalize_bands(Cexp.coeff, basis.n_device, norm_exp, self._norm_cut, self._i_iter, basis.n_max,
                                 basis.ke)

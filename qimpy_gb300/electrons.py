@@ -58,8 +58,9 @@ class Basis:
         self.grid_shape = tuple(int(x) for x in grid_shape)
         self.device = torch.device(device)
         self.dtype = dtype
-        #: Mixed form: subspace overlaps of complex64 vectors on the tensor cores
-        #: (split-BF16x3, qgb_dot_tc) instead of the FP32 CUDA-core Gram.
+        #: Mixed form: subspace overlaps and rotations of complex64 vectors on the
+        #: tensor cores (split-BF16x3, qgb_dot_tc / qgb_matmul_tc) instead of the
+        #: FP32 CUDA-core kernels.
         self.tc_subspace = False
         self.real = None  #: DeviceRealBasis of the real-wavefunction mode
         self.weight = None  #: FP64 overlap weights of the half basis (real mode)
@@ -223,8 +224,10 @@ class Wavefunction:
         return self  # norm-conserving: identity (_wavefunction_dot.py:127-134)
 
     def matmul(self, mat: torch.Tensor) -> "Wavefunction":
-        """C @ M along bands (qimpy/dft/electrons/_wavefunction_dot.py:137-191; qgb_matmul)."""
-        return Wavefunction(self.basis, coeff=ops.matmul(self.coeff, mat))
+        """C @ M along bands (qimpy/dft/electrons/_wavefunction_dot.py:137-191; qgb_matmul, or
+        qgb_matmul_tc for complex64 vectors of a basis with tc_subspace)."""
+        tc = self.basis.tc_subspace and self.coeff.dtype == torch.complex64
+        return Wavefunction(self.basis, coeff=ops.matmul(self.coeff, mat, tc=tc))
 
     __matmul__ = matmul
 

@@ -156,8 +156,10 @@ def dot(X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None, tc: b
     return out
 
 
-def matmul(C: torch.Tensor, M: torch.Tensor, out: torch.Tensor | None = None, accumulate: bool = False) -> torch.Tensor:
-    """out[k, j, g] (+)= sum_i M[k, i, j] C[k, i, g]; M is cast to C's dtype."""
+def matmul(C: torch.Tensor, M: torch.Tensor, out: torch.Tensor | None = None, accumulate: bool = False,
+           tc: bool = False) -> torch.Tensor:
+    """out[k, j, g] (+)= sum_i M[k, i, j] C[k, i, g]; M is cast to C's dtype.
+    tc=True (complex64 only): one split-BF16x3 tensor-core GEMM (qgb_matmul_tc)."""
     _check_block(C, "C")
     nk, n_in, n_tot = C.shape
     if M.dim() == 2:
@@ -178,8 +180,18 @@ def matmul(C: torch.Tensor, M: torch.Tensor, out: torch.Tensor | None = None, ac
         if not accumulate:
             out.zero_()
         return out
+    flags = _lib.QGB_ACCUMULATE if accumulate else 0
+    if tc:
+        if C.dtype != torch.complex64:
+            raise TypeError("the tensor-core rotation takes complex64 vectors")
+        lib = _lib.lib()
+        ws = workspace(lib.qgb_matmul_tc_workspace_bytes(nk, n_in, n_out, n_tot), C.device)
+        _lib.check(lib.qgb_matmul_tc(C.data_ptr(), n_in, nk, n_tot, Mc.data_ptr(), n_out, out.data_ptr(), flags,
+                                     ws.data_ptr(), ws.numel(), device_error_word(C.device).data_ptr(), _stream()),
+                   "matmul_tc")
+        return out
     _lib.check(_lib.lib().qgb_matmul(_qdtype(C), C.data_ptr(), n_in, nk, n_tot, Mc.data_ptr(), n_out, out.data_ptr(),
-                                     _lib.QGB_ACCUMULATE if accumulate else 0, _stream()), "matmul")
+                                     flags, _stream()), "matmul")
     return out
 
 

@@ -52,6 +52,25 @@ def test_dot_tensor_cores_match_numpy(nk, nx, ny, n):
     assert _err(got, want) < 5e-5
 
 
+@pytest.mark.parametrize("accumulate", [False, True])
+@pytest.mark.parametrize("nk,n_in,n_out,n", [(1, 7, 5, 33), (2, 130, 65, 1001), (1, 352, 176, 37073), (8, 36, 18, 1152)])
+def test_matmul_tensor_cores_match_numpy(nk, n_in, n_out, n, accumulate):
+    """qgb_matmul_tc (transposed split of C, split-BF16x3 GEMM accumulating into
+    out): within 5e-5 of the FP64 product (max-norm relative)."""
+    C = _rand((nk, n_in, n), 7, torch.complex64)
+    M = _rand((nk, n_in, n_out), 8, torch.complex64)
+    O = _rand((nk, n_out, n), 9, torch.complex64)
+    out = torch.from_numpy(O).to(DEV)
+    got = ops.matmul(torch.from_numpy(C).to(DEV), torch.from_numpy(M).to(DEV), out=out, accumulate=accumulate,
+                     tc=True).cpu().numpy()
+    torch.cuda.synchronize()
+    assert int(ops.device_error_word(DEV).item()) == 0
+    want = np.einsum("kij,kig->kjg", M.astype(np.complex128), C.astype(np.complex128))
+    if accumulate:
+        want = want + O
+    assert _err(got.astype(np.complex128), want) < 5e-5
+
+
 @pytest.mark.parametrize("dtype,tol", [(torch.complex128, 1e-13), (torch.complex64, 5e-6)])
 @pytest.mark.parametrize("nk,n_in,n_out,n", [(1, 7, 5, 33), (2, 130, 65, 1001), (1, 352, 176, 37073)])
 def test_matmul_matches_numpy(dtype, tol, nk, n_in, n_out, n):
