@@ -209,16 +209,25 @@ class Davidson:
             C_HC_new = _tile_expansion(C_HC, _sub((Cnew ^ HCexp).wait(), real))
             # FP32 vectors: directions the expanded basis barely spans are below
             # its rounding and are dropped (canonical orthogonalisation).
-            eig_new, V_new, failed = eighg(C_HC_new, C_OC_new, drop_below=1e-4 if fp32 else 0.0, check=False)
             n_bands_next = min(n_bands_new, n_bands_max)
-            # Everything the host needs from this iteration in one transfer:
-            # _check_deig (_davidson.py:126-139), the factorisation status and,
-            # for FP32, whether fewer usable directions than bands remain.
-            d = torch.abs(el.eig - eig_new[..., :n_bands_cur])[:, :n_bands]
-            pend = (d > self.eig_threshold).any(dim=0)
-            first_pending = torch.where(pend.any(), pend.int().argmax(), torch.tensor(n_bands, device=pend.device))
-            host = torch.stack((d.max(), first_pending.to(torch.float64), failed.any().to(torch.float64),
-                                torch.isinf(eig_new[:, n_bands_next - 1]).any().to(torch.float64))).tolist()
+            # FP32 vectors: the Cholesky path first; if its pivots call for the
+            # canonical orthogonalisation (known at the one host transfer of the
+            # iteration), the subspace problem is solved again that way.
+            for canonical in (False, True):
+                eig_new, V_new, failed, canon = eighg(C_HC_new, C_OC_new, drop_below=1e-4 if fp32 else 0.0,
+                                                      check=False, defer_canonical=True, force_canonical=canonical)
+                # Everything the host needs from this iteration in one transfer:
+                # _check_deig (_davidson.py:126-139), the factorisation status and,
+                # for FP32, whether fewer usable directions than bands remain.
+                d = torch.abs(el.eig - eig_new[..., :n_bands_cur])[:, :n_bands]
+                pend = (d > self.eig_threshold).any(dim=0)
+                first_pending = torch.where(pend.any(), pend.int().argmax(),
+                                            torch.full((), n_bands, dtype=torch.int64, device=pend.device))
+                host = torch.stack((d.max(), first_pending.to(torch.float64), failed.any().to(torch.float64),
+                                    torch.isinf(eig_new[:, n_bands_next - 1]).any().to(torch.float64),
+                                    canon.to(torch.float64))).tolist()
+                if not host[4]:
+                    break
             if host[2]:
                 raise RuntimeError("subspace eigenproblem failed: overlap not positive-definite or eigh did not converge")
             if fp32 and host[3]:
@@ -358,7 +367,8 @@ def _refine_mixed_expansion(el32: Electrons, el: Electrons, eig_threshold: float
         n_next = min(n_cur + n_exp, n_bands_max)
         d = torch.abs(el.eig - eig_new[..., :n_cur])[:, :n_bands]
         pend = (d > eig_threshold).any(dim=0)
-        first_pending = torch.where(pend.any(), pend.int().argmax(), torch.tensor(n_bands, device=pend.device))
+        first_pending = torch.where(pend.any(), pend.int().argmax(),
+                                    torch.full((), n_bands, dtype=torch.int64, device=pend.device))
         host = torch.stack((d.max(), first_pending.to(torch.float64), failed.any().to(torch.float64))).tolist()
         if host[2]:
             raise RuntimeError("refinement subspace problem failed: overlap not positive-definite")

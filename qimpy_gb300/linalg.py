@@ -84,7 +84,8 @@ def _canonical_ortho(O: torch.Tensor, drop_below: float):
     return V * scale[..., None, :].to(V.dtype), keep
 
 
-def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0, check: bool = True):
+def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0, check: bool = True,
+          defer_canonical: bool = False, force_canonical: bool = False):
     """Solve H V = O V E (qimpy/math/_linalg.py:143-183); H may be a Waitable.
 
     drop_below > 0 is for overlaps of FP32 vectors.  Their rounding (and the
@@ -99,17 +100,31 @@ def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0
     check=False returns (E, V, failed) with `failed` a device bool per k (a
     failed Cholesky factorisation of O, or an eigensolve that did not
     converge), so that the caller can fold the test into its own host
-    synchronisation; check=True raises as the reference does."""
+    synchronisation; check=True raises as the reference does.
+
+    defer_canonical=True (with drop_below > 0, check=False) takes the Cholesky
+    path without deciding on the host and returns (E, V, failed, canonical):
+    `canonical` is a device bool that is set when the pivots call for the
+    canonical orthogonalisation; the caller then solves again with
+    force_canonical=True.  The common case thus needs no host synchronisation."""
     Hr = H.wait() if hasattr(H, "wait") else H
     keep = None
     chol_failed = None
     if use_cholesky:
         eye = torch.eye(O.shape[-1], device=O.device, dtype=O.dtype).expand(O.shape)
-        L, info = torch.linalg.cholesky_ex(O)
-        if drop_below > 0.0:
+        canonical_flag = None
+        if force_canonical:
+            U, keep = _canonical_ortho(O, drop_below)
+            L, info = None, torch.zeros(O.shape[:-2], dtype=torch.int32, device=O.device)
+        else:
+            L, info = torch.linalg.cholesky_ex(O)
+        if drop_below > 0.0 and not force_canonical:
             pivot = L.diagonal(dim1=-2, dim2=-1).real.square().amin(dim=-1)
             floor = drop_below * O.diagonal(dim1=-2, dim2=-1).real.amax(dim=-1)
-            if bool(((info != 0) | (pivot < floor)).any()):
+            bad = ((info != 0) | (pivot < floor)).any()
+            if defer_canonical:
+                canonical_flag = bad
+            elif bool(bad):
                 U, keep = _canonical_ortho(O, drop_below)
         elif check:
             bad = torch.nonzero(info).flatten().tolist()
@@ -137,4 +152,9 @@ def eighg(H, O: torch.Tensor, use_cholesky: bool = True, drop_below: float = 0.0
     if keep is not None:
         n_keep = keep.sum(dim=-1, keepdim=True)
         E = torch.where(torch.arange(E.shape[-1], device=E.device) >= n_keep, torch.full_like(E, math.inf), E)
-    return (E, U @ V) if check else (E, U @ V, failed)
+    if check:
+        return E, U @ V
+    if defer_canonical:
+        flag = canonical_flag if canonical_flag is not None else torch.zeros((), dtype=torch.bool, device=E.device)
+        return E, U @ V, failed, flag
+    return E, U @ V, failed
