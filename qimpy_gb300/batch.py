@@ -166,7 +166,8 @@ class Instance:
         basis.fft_index, basis.iG, basis.tables, basis.sphere = self.layout.fft_index, self.layout.iG, \
             self.tables, self.sphere
         basis.ke = torch.from_numpy(self.layout.ke).to(self.sphere.device)
-        basis.real, basis.weight, basis.tc_subspace = None, None, False  # complex wavefunctions
+        basis.real, basis.weight = None, None  # complex wavefunctions
+        basis.tc_subspace = self.dtype == torch.complex64  # mixed: subspace products on the tensor cores
         pad = torch.arange(basis.n_tot)[None, :] < torch.from_numpy(basis.n)[:, None]
         basis.mask = pad.to(self.sphere.device)
         basis._V_id = id(self.V_r)

@@ -272,16 +272,16 @@ class Davidson:
 
 def refine_fp64(el_mixed: Electrons, el_fp64: Electrons, C: Optional[Wavefunction] = None,
                 eig_threshold: float = 1e-8, max_sweeps: int = 40, residual_threshold: Optional[float] = None,
-                method: str = "mixed_expansion", reset_every: int = 8):
+                method: str = "fp64_sweeps", reset_every: int = 8):
     """FP64 refinement of mixed-precision eigenvectors.
 
     Upcasts the vectors to complex128 and orthonormalises them (Cholesky,
     FP64).  FP32 H.psi leaves eigenvalues with noise near eps_f32 * Ecut
     (~1e-6 Ha); the sweeps below remove it.  Two methods:
 
-    * ``"fp64_sweeps"``: FP64 Davidson sweeps (the plain form's H.psi for the
-      current vectors and every expansion).
-    * ``"mixed_expansion"`` (default): FP64 H C once, then sweeps whose
+    * ``"fp64_sweeps"`` (default): FP64 Davidson sweeps (the plain form's H.psi
+      for the current vectors and every expansion).
+    * ``"mixed_expansion"``: FP64 H C once, then sweeps whose
       expansion vectors (the FP64 preconditioned residuals) go through the
       mixed H.psi only.  The Rayleigh-Ritz matrices are FP64: the coupling block
       C^H H X is formed as (H C)^H X from the carried FP64 H C, so it is exact

@@ -61,7 +61,7 @@ class Basis:
         #: Mixed form: subspace overlaps and rotations of complex64 vectors on the
         #: tensor cores (split-BF16x3, qgb_dot_tc / qgb_matmul_tc) instead of the
         #: FP32 CUDA-core kernels.
-        self.tc_subspace = False
+        self.tc_subspace = dtype == torch.complex64 and not real
         self.real = None  #: DeviceRealBasis of the real-wavefunction mode
         self.weight = None  #: FP64 overlap weights of the half basis (real mode)
         if real:
