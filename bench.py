@@ -598,7 +598,7 @@ def run_eigensolve_si64(args, local):
         res = dict(iterations=stats.iterations, converged=stats.converged, stalled=stats.stalled)
         if form == "mixed":
             res["max_eig_error_ha_before_refinement"] = float(np.abs(el.eig.cpu().numpy()[:, : p.n_bands] - ref).max())
-            eig, _ = dv.refine_fp64(el, el64, eig_threshold=1e-9)
+            eig, _ = dv.refine_fp64(el, el64, eig_threshold=1e-9, max_sweeps=150)
             res["refinement_sweeps"] = el64.last_refine.iterations
         else:
             eig = el.eig
