@@ -53,10 +53,26 @@ def test_poisson_stream_arrivals_and_band_caps():
     assert [(r.arrival, r.n_bands) for r in again] == [(r.arrival, r.n_bands) for r in reqs]
 
 
+def _fake_server(dtype, residual_threshold=None):
+    fake = types.SimpleNamespace(dtype=dtype, residual_threshold=residual_threshold)
+    fake.bands_extra = lambda nb, n_min: sv.EigenServer.bands_extra(fake, nb, n_min)
+    return fake
+
+
+def test_serving_extra_bands():
+    """The reference's default without a residual target; with one, at least 4
+    and a quarter of the bands, within Davidson's limit 2 (n_bands + extra) < n_min."""
+    plain, target = _fake_server(torch.complex64), _fake_server(torch.complex64, 1e-6)
+    assert [plain.bands_extra(nb, 10000) for nb in (6, 10, 11, 160)] == [1, 1, 2, 16]
+    assert [target.bands_extra(nb, 10000) for nb in (6, 10, 40, 160)] == [4, 4, 10, 40]
+    assert target.bands_extra(6, 21) == 4 and target.bands_extra(6, 19) == 3  # capped: 2 (6 + 3) < 19
+    assert target.bands_extra(8, 17) == 1  # never below the reference's default
+
+
 def test_serving_memory_estimate_grows_with_work():
     spec = bt.make_batch_specs(count=1, seed=3)[0]
-    fake = types.SimpleNamespace(dtype=torch.complex64)
-    fake64 = types.SimpleNamespace(dtype=torch.complex128)
+    fake = _fake_server(torch.complex64)
+    fake64 = _fake_server(torch.complex128)
     small = sv.EigenServer.estimate_bytes(fake, spec, 8)
     large = sv.EigenServer.estimate_bytes(fake, spec, 64)
     assert 0 < small < large
