@@ -49,6 +49,8 @@ class EigenRequest:
     hpsi_bands: int = 0
     converged: bool = False
     residual: float = math.nan
+    t_solved: float = math.nan  #: the batched Davidson finished (refinement and checks follow)
+    refine_sweeps: int = 0  #: FP64 refinement sweeps of a mixed solve
 
     @property
     def latency(self) -> float:
@@ -344,6 +346,7 @@ class EigenServer:
         refinement of a mixed solve, the final residual
         max_b ||H psi_b - eps_b psi_b|| (one more H.psi), result checks, latency."""
         req = a.req
+        req.t_solved = now_fn()
         try:
             with torch.cuda.stream(a.stream):
                 self._finish_solve(a, stats)
@@ -364,6 +367,7 @@ class EigenServer:
             refine_fp64(el, el64, eig_threshold=self.refine_threshold, residual_threshold=self.residual_threshold,
                         max_sweeps=max(40, self.max_iterations - stats.iterations))
             ref = el64.last_refine
+            req.refine_sweeps = ref.iterations
             req.hpsi_bands += ref.hpsi_bands
             iterations += ref.iterations
             converged = (converged or stats.stalled) and (ref.converged or ref.deig_max <= self.eig_threshold)
