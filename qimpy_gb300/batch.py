@@ -167,7 +167,11 @@ class Instance:
             self.tables, self.sphere
         basis.ke = torch.from_numpy(self.layout.ke).to(self.sphere.device)
         basis.real, basis.weight = None, None  # complex wavefunctions
-        basis.tc_subspace = self.dtype == torch.complex64  # mixed: subspace products on the tensor cores
+        # Subspace products on the CUDA cores: the tensor-core ones take ~0.2 GB
+        # of bf16 operand workspace per call on the largest cells, and with many
+        # requests' worker threads each caching its own, served runs exhausted
+        # device memory (library handle creation then failed).
+        basis.tc_subspace = False
         pad = torch.arange(basis.n_tot)[None, :] < torch.from_numpy(basis.n)[:, None]
         basis.mask = pad.to(self.sphere.device)
         basis._V_id = id(self.V_r)
