@@ -88,7 +88,10 @@ class Instance:
     """Device-resident data of one instance (complex64 by default)."""
 
     def __init__(self, spec: InstanceSpec, device, fft_factors=None, tune: bool = False,
-                 dtype: torch.dtype = torch.complex64):
+                 dtype: torch.dtype = torch.complex64, real: bool = False):
+        """real=True (Gamma-only specs): real wavefunctions on the half basis
+        (qimpy/dft/electrons/_basis_real.py), the transforms on the full Gamma
+        sphere with two real bands per complex transform."""
         self.spec = spec
         dev = torch.device(device)
         L, shape = spec.side, (spec.grid,) * 3
@@ -98,10 +101,22 @@ class Instance:
             fft_factors = tune_shape(shape, torch.complex64, dev)
         R = np.eye(3) * L
         Gb = 2.0 * np.pi * np.linalg.inv(R.T)
-        self.layout = wl.make_basis_device(Gb, spec.k, spec.ke_cutoff, shape, dev)
-        self.tables = sp.build_tables(self.layout.fft_index, self.layout.n, shape, fft_factors)
         self.dtype = dtype
-        self.sphere = sp.DeviceSphere(self.tables, self.layout.ke, dev, dtype)
+        self.real_basis = None
+        if real:
+            from .real_basis import DeviceRealBasis, gamma_bases
+
+            if spec.k.shape[0] != 1 or np.any(spec.k != 0.0):
+                raise ValueError("real wavefunctions need a Gamma-only instance")
+            half, full = gamma_bases(Gb, spec.ke_cutoff, shape)
+            self.real_basis = DeviceRealBasis(half, full, dev, dtype, fft_factors)
+            self.layout = half
+            self.sphere = self.real_basis.sphere
+            self.tables = self.sphere.tables
+        else:
+            self.layout = wl.make_basis_device(Gb, spec.k, spec.ke_cutoff, shape, dev)
+            self.tables = sp.build_tables(self.layout.fft_index, self.layout.n, shape, fft_factors)
+            self.sphere = sp.DeviceSphere(self.tables, self.layout.ke, dev, dtype)
         self.Rbasis, self.fft_factors = R, self.tables.fac
         self.nk, self.nb, self.n_tot = spec.k.shape[0], spec.n_bands, self.layout.n_tot
         self.volume = L ** 3
@@ -166,7 +181,8 @@ class Instance:
         basis.fft_index, basis.iG, basis.tables, basis.sphere = self.layout.fft_index, self.layout.iG, \
             self.tables, self.sphere
         basis.ke = torch.from_numpy(self.layout.ke).to(self.sphere.device)
-        basis.real, basis.weight = None, None  # complex wavefunctions
+        basis.real = self.real_basis
+        basis.weight = self.real_basis.weight if self.real_basis is not None else None
         # Subspace products on the CUDA cores: the tensor-core ones take ~0.2 GB
         # of bf16 operand workspace per call on the largest cells, and with many
         # requests' worker threads each caching its own, served runs exhausted
@@ -192,7 +208,10 @@ class Instance:
                                              device=self.sphere.device)).to(self.dtype)
             more = (more / (1 + basis.ke[:, None, :]) * basis.mask[:, None, :]).to(self.dtype)
             C = torch.cat((C, more), dim=1)
-        el.C = E.Wavefunction(basis, coeff=C.contiguous()).orthonormalize()
+        C = E.Wavefunction(basis, coeff=C.contiguous())
+        if self.real_basis is not None:
+            C.constrain()  # Hermitian Gz = 0 plane
+        el.C = C.orthonormalize()
         return el
 
     @property

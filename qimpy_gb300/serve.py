@@ -78,14 +78,16 @@ class EigenServer:
     def __init__(self, device="cuda", precision: str = "mixed", hbm_budget_bytes: int = 160 << 30,
                  max_active: int = 64, eig_threshold: float = 1e-6, residual_threshold: Optional[float] = None,
                  max_iterations: int = 200, refine: bool = True, refine_threshold: Optional[float] = None,
-                 workers: int = 16):
+                 workers: int = 16, real_gamma: bool = True):
         """eig_threshold: Davidson's stop on the largest eigenvalue change (Ha);
         refine_threshold: the same for the FP64 refinement of a mixed solve
         (default eig_threshold / 10); a refinement that ends
         above it but within eig_threshold still completes the request;
         residual_threshold: optional extra stop on the FP64 residual norm
         (FP64 solve, or the refinement).  Every finished request reports its
-        final residual."""
+        final residual.  real_gamma: Gamma-only requests use real wavefunctions
+        on the half basis (qimpy/dft/electrons/_basis_real.py); their H.psi runs
+        per request rather than in the batched launches."""
         if precision not in ("mixed", "fp64"):
             raise ValueError("precision must be 'mixed' or 'fp64'")
         self.device = torch.device(device)
@@ -99,6 +101,7 @@ class EigenServer:
         self.max_iterations = max_iterations
         self.refine = refine and precision == "mixed"
         self.refine_threshold = refine_threshold if refine_threshold is not None else eig_threshold / 10
+        self.real_gamma = real_gamma
         self.queue: list = []
         self.active: list = []
         self.finished: list = []
@@ -192,7 +195,7 @@ class EigenServer:
         stream.wait_stream(main)
         try:
             with torch.cuda.stream(stream):
-                inst = Instance(req.spec, self.device, dtype=self.dtype)
+                inst = Instance(req.spec, self.device, dtype=self.dtype, real=self._real(req.spec))
                 n_min = int(inst.layout.n.min())
                 extra = self.bands_extra(req.n_bands, n_min)
                 nbt = req.n_bands + extra
@@ -204,14 +207,17 @@ class EigenServer:
                                residual_threshold=None if precision_is_mixed else self.residual_threshold)
                 gen = dav.steps()
                 block = next(gen)
-                planes = torch.empty(inst.sphere.workspace_bytes(el.C.n_bands(), budget=1 << 62), dtype=torch.uint8,
-                                     device=self.device)
+                planes = torch.empty(inst.sphere.workspace_bytes(el.C.n_bands(), budget=1 << 62)
+                                     if inst.real_basis is None else 1, dtype=torch.uint8, device=self.device)
                 sd = torch.frombuffer(bytearray(bytes(inst.sphere.struct)), dtype=torch.uint8).to(self.device)
                 ready = torch.cuda.Event()
                 ready.record(stream)
             return inst, el, gen, block, planes, sd, stream, ready
         except (ValueError, RuntimeError, torch.cuda.OutOfMemoryError) as e:
             return e
+
+    def _real(self, spec: InstanceSpec) -> bool:
+        return self.real_gamma and spec.k.shape[0] == 1 and not np.any(spec.k != 0.0)
 
     def bands_extra(self, n_bands: int, n_min: int) -> int:
         """Bands kept beyond the requested ones.  Without a residual target this
@@ -238,6 +244,12 @@ class EigenServer:
         of all requests sharing a grid shape in three batched launches, then each
         request's nonlocal term."""
         lib = _lib.lib()
+        real = [i for i, a in enumerate(acts) if a.inst.real_basis is not None]
+        if real:  # real-wavefunction requests: their own H.psi calls
+            outs_real = {i: acts[i].el.hamiltonian(acts[i].block) for i in real}
+            rest = [a for a in acts if a.inst.real_basis is None]
+            outs_rest = iter(self._batched_hamiltonian(rest)) if rest else iter(())
+            return [outs_real[i] if i in outs_real else next(outs_rest) for i in range(len(acts))]
         for a in acts:  # the kernels read every block with the server's element type
             c = a.block.coeff
             if c.dtype != self.dtype or not c.is_contiguous() or c.shape[0] != a.inst.nk or c.shape[2] != a.inst.n_tot:
@@ -362,7 +374,7 @@ class EigenServer:
         if self.refine:
             # A mixed solve that stopped at FP32's floor (stalled) is finished
             # by the FP64 sweeps.
-            inst64 = Instance(req.spec, self.device, dtype=torch.complex128)
+            inst64 = Instance(req.spec, self.device, dtype=torch.complex128, real=a.inst.real_basis is not None)
             el64 = inst64.electrons(req.n_bands, el.n_bands_extra)
             refine_fp64(el, el64, eig_threshold=self.refine_threshold, residual_threshold=self.residual_threshold,
                         max_sweeps=max(40, self.max_iterations - stats.iterations))
@@ -375,7 +387,7 @@ class EigenServer:
                 why = why or f"FP64 refinement not converged in {ref.iterations} sweeps (deig_max {ref.deig_max:.2e})"
             el = el64
         HC = el.hamiltonian(el.C)
-        res = ops.residual(HC.coeff, el.C.coeff, el.eig.contiguous(), norm=True)
+        res = ops.residual(HC.coeff, el.C.coeff, el.eig.contiguous(), norm=True, weight=el.basis.weight)
         req.residual = float(res[:, : req.n_bands].max())
         if converged and self.residual_threshold is not None and not req.residual < self.residual_threshold:
             converged = False
