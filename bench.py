@@ -59,7 +59,8 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=256, help="instances of the batched workload (0 = skip)")
     ap.add_argument("--batch-chunk-mb", type=int, default=0,
                     help="slab-plane MB per batched launch chunk (0 = one chunk per grid shape)")
-    ap.add_argument("--serve", type=int, default=32, help="requests of the serving stream sample (0 = skip)")
+    ap.add_argument("--serve", type=int, default=16,
+                    help="requests of the serving stream sample, the same for both forms (0 = skip)")
     ap.add_argument("--serve-wall", type=float, default=150.0, help="wall-clock cap per serving run (s)")
     ap.add_argument("--no-eigensolve", action="store_true")
     ap.add_argument("--profile-davidson", action="store_true",
@@ -754,16 +755,16 @@ def run_serving(args, local):
     below 1e-6 Ha; mixed requests then refined in FP64 to 1e-8 Ha),
     cells drawn from the batched-instance distribution plus 5% 64-atom Si-like
     cells (side 20.52 bohr, 96^3, Ecut 20 Ha).  Mixed precision (FP32 H.psi,
-    tensor-core nonlocal, FP64 subspace and refinement) and plain FP64; a
-    bounded sample of the stream (`--serve` requests mixed, a quarter of that
-    FP64) keeps the run within minutes."""
+    tensor-core nonlocal, FP64 subspace and refinement) and plain FP64 on the
+    same bounded sample of the stream (`--serve` requests each), which keeps
+    the run within minutes.  Gamma-only requests run with real wavefunctions."""
     import torch
 
     from qimpy_gb300 import batch as bt, serve as sv, workloads as wl
 
     dev = torch.device(f"cuda:{local}")
     out = {}
-    for precision, count in (("mixed", args.serve), ("fp64", max(4, args.serve // 4))):
+    for precision, count in (("mixed", args.serve), ("fp64", args.serve)):
         specs = bt.make_batch_specs(count=count, seed=41)
         u = wl.splitmix_uniform(41, 900, count)
         for i in range(count):
