@@ -257,10 +257,15 @@ class Davidson:
                 HC = yield el.C
                 hpsi_bands += el.C.n_bands() * el.basis.nk
                 res = ops.residual(HC.coeff, el.C.coeff, el.eig, norm=True, weight=w)
-                res_max = float(res[:, :n_bands].max())
+                res_band = res[:, :n_bands].amax(dim=0)  # worst k-point per band
+                host_res = torch.stack((res_band.max(), (res_band >= self.residual_threshold).int().argmax()
+                                        .to(torch.float64))).tolist()
+                res_max = host_res[0]
                 if res_max >= self.residual_threshold:
                     converged = False
-                    n_eigs_done = 0  # eigenvalues settled, residuals not yet: keep all bands active
+                    # Eigenvalues settled, residuals not yet: the bands below the
+                    # first one above the target stay converged; the rest expand.
+                    n_eigs_done = int(host_res[1])
             if converged:
                 break
             if fp32 and self._i_iter - i_best >= 10:
