@@ -288,11 +288,12 @@ __device__ __forceinline__ void xmid_dispatch(int L1, cplx_t<T>* sm, int p, int 
   }
 }
 
-// x-pass with asynchronous staging (FP32, N2 % 4 == 0): the slab rows and the
-// CTA's V slice are copied to shared memory with cp.async (no register
-// staging); V streams in while the first inverse pass runs, so the middle
-// step reads only shared memory.  Shared layout: pencils [N0][ldx = N2 + 2]
-// complex, W_x [N0] complex, V slice [N0][N2] real.
+// x-pass with asynchronous staging (FP32, N2 % 4 == 0): the slab rows are
+// copied to shared memory with cp.async (no register staging).  The middle
+// step reads V(r) from global memory (it stays in L2 across the bands), which
+// keeps shared memory at 75 KB for si64 (96^3) so that 3 CTAs fit an SM;
+// staging the V slice as well (111 KB, 2 CTAs) made the local apply 6%
+// slower.  Shared layout: pencils [N0][ldx = N2 + 2] complex, W_x [N0] complex.
 template <typename T>
 __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const LocalParams& lp,
                                                  cplx_t<T>* __restrict__ planes, const int r1, const int b,
@@ -302,7 +303,6 @@ __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const Loca
   const int L1 = s.L1[0], L2 = s.L2[0];
   const int lim = N0 * ld, Wx = lim;
   C2* sm = smem_c<T>();
-  T* Vs = reinterpret_cast<T*>(sm + ((Wx + N0 + 1) & ~1));  // 16-byte aligned for cp.async
   const C2* tw = static_cast<const C2*>(s.twiddle);
   load_twiddles<T>(Wx, tw + s.tw_off[0], N0);
   const C2 zero = mk<T>(T(0), T(0));
@@ -315,33 +315,27 @@ __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const Loca
   const int* i0 = s.slab_i0 + k * s.max_slabs;
   const size_t plane = static_cast<size_t>(N1) * N2;
   C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2 + z0;
-  // Group 1: slab rows, columns [z0, z0 + nz) (16 B = 2 complex per copy).
+  // Slab rows, columns [z0, z0 + nz) (16 B = 2 complex per copy).
   const int cpr = nz / 2;  // copies per row
   for (int it = threadIdx.x; it < nslabs * cpr; it += blockDim.x) {
     const int sl = it / cpr, c = 2 * (it - sl * cpr);
     cp_async16(sm + i0[sl] * ld + c, base + sl * plane + c);
   }
   cp_async_commit();
-  // Group 2: V slice V[p0][r1][z0 .. z0 + nz) for all p0 (16 B = 4 reals per copy).
-  const T* V = static_cast<const T*>(s.V);
-  const int vpr = nz / 4;
-  for (int it = threadIdx.x; it < N0 * vpr; it += blockDim.x) {
-    const int p0 = it / vpr, c = 4 * (it - p0 * vpr);
-    cp_async16(Vs + p0 * nz + c, V + (static_cast<size_t>(p0) * N1 + r1) * N2 + z0 + c);
-  }
-  cp_async_commit();
-  cp_async_wait<1>();
+  cp_async_wait<0>();
   __syncthreads();
 
   if (L2 > 1) {
     run_pass<T, +1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
+    __syncthreads();
   }
-  cp_async_wait<0>();
-  __syncthreads();
+  // V[p0][r1][z0 + c] with p0 = a * L1 + j: j-stride N1 * N2.
+  const T* V = static_cast<const T*>(s.V) + static_cast<size_t>(r1) * N2 + z0;
   for (int it = threadIdx.x; it < nz * L2; it += blockDim.x) {
     const int a = it / nz;
     const int c = it - a * nz;
-    xmid_dispatch<T>(L1, sm, c + a * L1 * ld, ld, Vs + a * L1 * nz + c, static_cast<size_t>(nz), Wx, L2, a);
+    xmid_dispatch<T>(L1, sm, c + a * L1 * ld, ld, V + static_cast<size_t>(a) * L1 * N1 * N2 + c,
+                     static_cast<size_t>(N1) * N2, Wx, L2, a);
   }
   __syncthreads();
   if (L2 > 1) {
@@ -438,7 +432,7 @@ __global__ void __launch_bounds__(kThreads) k_xpass(const qgb_sphere s, LocalPar
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_xpass_async(const qgb_sphere s, LocalParams lp,
+__global__ void __launch_bounds__(kThreads, 3) k_xpass_async(const qgb_sphere s, LocalParams lp,
                                                           cplx_t<T>* __restrict__ planes) {
   body_xpass_async<T>(s, lp, planes, blockIdx.x, blockIdx.y, blockIdx.z, 0, s.N[2]);
 }
@@ -592,7 +586,7 @@ static bool xpass_async_ok(const qgb_sphere& s, int dtype) { return dtype == QGB
 
 static size_t xpass_async_smem_bytes(const qgb_sphere& s) {
   const size_t cplx = (static_cast<size_t>(s.N[0]) * (s.N[2] + 2) + s.N[0] + 1) & ~static_cast<size_t>(1);
-  return cplx * 8 + static_cast<size_t>(s.N[0]) * s.N[2] * 4;
+  return cplx * 8;
 }
 
 int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true) {
