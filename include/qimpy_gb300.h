@@ -436,8 +436,10 @@ int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, in
  * The same in two phases, so that the part that reads only C can run beside
  * the local potential (another stream): phases = 1 computes projT and the
  * back-projection operand in `workspace` (HC untouched), phases = 2 then does
- * HC += beta (D projT) from that workspace, phases = 3 both.  Between a
- * phase-1 and its phase-2 call the workspace must not be reused.
+ * HC += beta (D projT) from that workspace, phases = 3 both.  Adding 4 to a
+ * phases value that includes 2 stores HC = beta (D projT) instead of adding
+ * (every entry of HC, padding included, is written).  Between a phase-1 and
+ * its phase-2 call the workspace must not be reused.
  */
 int qgb_apply_nonlocal_tc_phase(const void* beta_split, const void* D, int n_atoms, int pa, const void* C,
                                 void* HC, void* projT, int nk, int nb, int n_tot, void* workspace,
@@ -445,10 +447,14 @@ int qgb_apply_nonlocal_tc_phase(const void* beta_split, const void* D, int n_ato
 
 /*
  * Mixed-precision H C (complex64): FP32 KE + local potential (as
- * qgb_apply_potential with QGB_ADD_KE), then the tensor-core nonlocal term
+ * qgb_apply_potential with QGB_ADD_KE) plus the tensor-core nonlocal term
  * (qgb_apply_nonlocal_tc); replaces Electrons.hamiltonian,
- * qimpy/dft/electrons/_hamiltonian.py:7-29, in the mixed form.  beta_split
- * comes from qgb_beta_split; workspace of qgb_hamiltonian_mixed_workspace_bytes.
+ * qimpy/dft/electrons/_hamiltonian.py:7-29, in the mixed form.  The nonlocal
+ * term runs on a library side stream (forked from and joined back to `stream`
+ * by events, so the call can be captured) and is stored into HC while the
+ * local potential's transforms run; the local potential's last kernel then
+ * adds KE C + V C.  beta_split comes from qgb_beta_split; workspace of
+ * qgb_hamiltonian_mixed_workspace_bytes.
  */
 size_t qgb_hamiltonian_mixed_workspace_bytes(const qgb_sphere* s, int nb, int P);
 int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, const void* beta_split,

@@ -48,7 +48,8 @@ int raise_smem_limit(const void* kernel, size_t bytes) {
 int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true);
 size_t plane_bytes_per_band(const qgb_sphere& s, int dtype);
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
-                    void* ws, size_t ws_bytes, cudaStream_t st);
+                    void* ws, size_t ws_bytes, cudaStream_t st,
+                    cudaEvent_t gather_after = nullptr);
 int apply_ke(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, cudaStream_t st);
 size_t project_workspace_bytes(int dtype, int nk, int P, int nb, int n_tot);
 int project(int dtype, const void* beta, const void* C, void* projT, int nk, int P, int nb, int n_tot, void* ws,
@@ -83,7 +84,8 @@ int gram_tc(const void* X, int nx, const void* Y, int ny, int nk, int n, double2
             int oj, void* ws, size_t ws_bytes, int* err, cudaStream_t st);
 size_t real_local_bytes(const qgb_sphere& full, const qgb_real_map& m, int nb, int dtype);
 int real_local(const qgb_sphere* full, const qgb_real_map* m, int dtype, const void* C, void* HC, int nb, void* ws,
-               size_t ws_bytes, cudaStream_t st);
+               size_t ws_bytes, cudaStream_t st,
+               cudaEvent_t unpack_after = nullptr);
 
 // A side stream and a fork/join event pair per (host thread, device): the mixed
 // Hamiltonian runs the C-only part of its nonlocal term there, beside the local
@@ -304,7 +306,8 @@ int qgb_apply_nonlocal_tc(const void* beta_split, const void* D, int n_atoms, in
 int qgb_apply_nonlocal_tc_phase(const void* beta_split, const void* D, int n_atoms, int pa, const void* C,
                                 void* HC, void* projT, int nk, int nb, int n_tot, void* workspace,
                                 size_t workspace_bytes, int* dev_error, int phases, void* stream) {
-  if (phases < 1 || phases > 3) return fail(QGB_ERR_INVALID, "phases = %d (1, 2 or 3)", phases);
+  if (phases < 1 || phases > 7 || phases == 4 || phases == 5)
+    return fail(QGB_ERR_INVALID, "phases = %d (1, 2 or 3, plus 4 with 2)", phases);
   return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, nk, nb, n_tot, workspace, workspace_bytes,
                            dev_error, phases, static_cast<cudaStream_t>(stream));
 }
@@ -329,19 +332,22 @@ int qgb_hamiltonian_mixed(const qgb_sphere* s, const void* C, void* HC, int nb, 
   if (P == 0 || nb == 0) return apply_potential(s, QGB_F32, C, HC, nb, QGB_ADD_KE, ws + nl, workspace_bytes - nl, st);
   SideStream f;
   if ((rc = side_stream(&f))) return rc;
-  // Fork: the projection (split, <beta|psi>, reduce, D) on the side stream...
+  // Fork: the whole nonlocal term on the side stream (split, <beta|psi>,
+  // reduce, D, and the back-projection storing HC = beta (D projT)) while the
+  // inverse and x passes of the local potential run; their gather kernels wait
+  // for it and accumulate KE C + V C into HC.  The nonlocal chain is thus off
+  // the critical path.  The join is waited for on every path, so that a
+  // capture stays well-formed even when a launch was refused.
   QGB_CUDA_CHECK(cudaEventRecord(f.fork, st));
   QGB_CUDA_CHECK(cudaStreamWaitEvent(f.side, f.fork, 0));
   const int rc_front = nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl,
-                                         dev_error, 1, f.side);
-  // ...joined back before the back-projection accumulates into HC (always, so
-  // that a capture stays well-formed even when a launch was refused).
+                                         dev_error, 1 | 2 | 4, f.side);
   QGB_CUDA_CHECK(cudaEventRecord(f.join, f.side));
-  rc = apply_potential(s, QGB_F32, C, HC, nb, QGB_ADD_KE, ws + nl, workspace_bytes - nl, st);
+  rc = apply_potential(s, QGB_F32, C, HC, nb, QGB_ADD_KE | QGB_ACCUMULATE, ws + nl, workspace_bytes - nl, st,
+                       f.join);
   QGB_CUDA_CHECK(cudaStreamWaitEvent(st, f.join, 0));
   if (rc_front) return rc_front;
-  if (rc) return rc;
-  return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, s->nk, nb, s->n_tot, ws, nl, dev_error, 2, st);
+  return rc;
 }
 
 size_t qgb_hamiltonian_real_mixed_workspace_bytes(const qgb_sphere* full, const qgb_real_map* map, int nb, int P) {
@@ -370,19 +376,18 @@ int qgb_hamiltonian_real_mixed(const qgb_sphere* full, const qgb_real_map* map, 
   if (P == 0) return real_local(full, map, QGB_F32, C, HC, nb, ws, workspace_bytes, st);
   SideStream f;
   if ((rc = side_stream(&f))) return rc;
-  // As qgb_hamiltonian_mixed: the weighted real projection on the side stream
-  // beside the local potential, joined before the back-projection.
+  // As qgb_hamiltonian_mixed: the whole nonlocal term (weighted real
+  // projection, D, back-projection stored into HC) on the side stream beside
+  // the local potential, whose unpack waits for it and adds KE C + V C.
   QGB_CUDA_CHECK(cudaEventRecord(f.fork, st));
   QGB_CUDA_CHECK(cudaStreamWaitEvent(f.side, f.fork, 0));
   const int rc_front = nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, 1, nb, map->n_tot_half, ws, nl,
-                                         dev_error, 1, f.side, map->weight);
+                                         dev_error, 1 | 2 | 4, f.side, map->weight);
   QGB_CUDA_CHECK(cudaEventRecord(f.join, f.side));
-  rc = real_local(full, map, QGB_F32, C, HC, nb, ws + nl, workspace_bytes - nl, st);
+  rc = real_local(full, map, QGB_F32, C, HC, nb, ws + nl, workspace_bytes - nl, st, f.join);
   QGB_CUDA_CHECK(cudaStreamWaitEvent(st, f.join, 0));
   if (rc_front) return rc_front;
-  if (rc) return rc;
-  return nonlocal_tc_phase(beta_split, D, n_atoms, pa, C, HC, projT, 1, nb, map->n_tot_half, ws, nl, dev_error, 2,
-                           st, map->weight);
+  return rc;
 }
 
 }  // extern "C"

@@ -73,6 +73,151 @@ __device__ __forceinline__ void cp_async_elem(cplx_t<T>* smem_dst, const cplx_t<
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// y passes of the y/z kernels with the plane's boundaries folded in (used when
+// both y factors exceed 1).  Rows y of the shared plane sit at offset y * ld,
+// columns c < nz; `rowmask[y]` marks the rows the slab's sphere points touch.
+// ---------------------------------------------------------------------------
+
+// Inverse pass 1 (radix R = L2) over rows sub + j * L1 with the pass-1
+// twiddles; untouched rows are read as zero (they are never zero-filled).
+template <typename T, int R>
+__device__ __forceinline__ void ypass_inv1_R(const int* rowmask, int nz, int L1, int ld, int W, int lim) {
+  cplx_t<T>* sm = smem_c<T>();
+  const int nitems = nz * L1;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int sub = it / nz;
+    const int c = it - sub * nz;
+    T re[R], im[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int y = sub + j * L1;
+      const int off = y * ld + c;
+      if (!QGB_OK_IDX(off, lim, 64)) return;
+      cplx_t<T> v = mk<T>(T(0), T(0));
+      if (rowmask[y]) v = sm[off];
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    Codelet<R, +1>::run(re, im);
+#pragma unroll
+    for (int j = 1; j < R; ++j) {
+      const cplx_t<T> w = sm[W + sub * R + j];
+      const T xr = re[j] * w.x - im[j] * w.y;
+      const T xi = re[j] * w.y + im[j] * w.x;
+      re[j] = xr;
+      im[j] = xi;
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) sm[(sub + j * L1) * ld + c] = mk<T>(re[j], im[j]);
+  }
+}
+
+// Inverse pass 2 (radix R = L1) over rows sub * L1 + j, stored straight to the
+// plane in global memory (row stride N2), in the permuted order of the rows.
+template <typename T, int R>
+__device__ __forceinline__ void ypass_inv2_R(cplx_t<T>* __restrict__ out, int N2, int nz, int L2, int ld, int lim) {
+  cplx_t<T>* sm = smem_c<T>();
+  const int nitems = nz * L2;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int sub = it / nz;
+    const int c = it - sub * nz;
+    T re[R], im[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int off = (sub * R + j) * ld + c;
+      if (!QGB_OK_IDX(off, lim, 65)) return;
+      const cplx_t<T> v = sm[off];
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    Codelet<R, +1>::run(re, im);
+#pragma unroll
+    for (int j = 0; j < R; ++j) out[static_cast<size_t>(sub * R + j) * N2 + c] = mk<T>(re[j], im[j]);
+  }
+}
+
+// Forward pass A (radix R = L1) over rows a * L1 + j, read straight from the
+// plane in global memory, times the conjugated pass-A twiddles.
+template <typename T, int R>
+__device__ __forceinline__ void ypass_fwdA_R(const cplx_t<T>* __restrict__ in, int N2, int nz, int L2, int ld, int W,
+                                             int lim) {
+  cplx_t<T>* sm = smem_c<T>();
+  const int nitems = nz * L2;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int a = it / nz;
+    const int c = it - a * nz;
+    T re[R], im[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const cplx_t<T> v = in[static_cast<size_t>(a * R + j) * N2 + c];
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    Codelet<R, -1>::run(re, im);
+#pragma unroll
+    for (int j = 1; j < R; ++j) {
+      const cplx_t<T> w = sm[W + a + j * L2];
+      const T xr = re[j] * w.x + im[j] * w.y;
+      const T xi = im[j] * w.x - re[j] * w.y;
+      re[j] = xr;
+      im[j] = xi;
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int off = (a * R + j) * ld + c;
+      if (!QGB_OK_IDX(off, lim, 66)) return;
+      sm[off] = mk<T>(re[j], im[j]);
+    }
+  }
+}
+
+// Forward pass B (radix R = L2) over rows sub + j * L1 (natural order out);
+// only the rows the slab's sphere points touch are stored.
+template <typename T, int R>
+__device__ __forceinline__ void ypass_fwdB_R(const int* rowmask, int nz, int L1, int ld, int lim) {
+  cplx_t<T>* sm = smem_c<T>();
+  const int nitems = nz * L1;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int sub = it / nz;
+    const int c = it - sub * nz;
+    T re[R], im[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int off = (sub + j * L1) * ld + c;
+      if (!QGB_OK_IDX(off, lim, 67)) return;
+      const cplx_t<T> v = sm[off];
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    Codelet<R, -1>::run(re, im);
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+      if (rowmask[sub + j * L1]) sm[(sub + j * L1) * ld + c] = mk<T>(re[j], im[j]);
+  }
+}
+
+// kind 0: inverse pass 1; 1: inverse pass 2 (to global); 2: forward pass A
+// (from global); 3: forward pass B.  R is the pass's radix.
+template <typename T, int KIND>
+__device__ __forceinline__ void ypass(int R, const int* rowmask, cplx_t<T>* g, int N2, int nz, int L1, int L2,
+                                      int ld, int W, int lim) {
+#define QGB_YP(RR)                                                                  \
+  case RR:                                                                          \
+    if constexpr (KIND == 0) ypass_inv1_R<T, RR>(rowmask, nz, L1, ld, W, lim);      \
+    if constexpr (KIND == 1) ypass_inv2_R<T, RR>(g, N2, nz, L2, ld, lim);           \
+    if constexpr (KIND == 2) ypass_fwdA_R<T, RR>(g, N2, nz, L2, ld, W, lim);        \
+    if constexpr (KIND == 3) ypass_fwdB_R<T, RR>(rowmask, nz, L1, ld, lim);         \
+    break;
+  switch (R) {
+    QGB_YP(2) QGB_YP(3) QGB_YP(4) QGB_YP(5) QGB_YP(6) QGB_YP(7) QGB_YP(8) QGB_YP(9) QGB_YP(10) QGB_YP(12)
+    QGB_YP(14) QGB_YP(15) QGB_YP(16)
+    default: break;
+  }
+#undef QGB_YP
+}
+
 template <typename T>
 __device__ __forceinline__ void body_ifft_yz(const qgb_sphere& s, const LocalParams& lp,
                                              const cplx_t<T>* __restrict__ C, cplx_t<T>* __restrict__ planes,
@@ -80,16 +225,39 @@ __device__ __forceinline__ void body_ifft_yz(const qgb_sphere& s, const LocalPar
   using C2 = cplx_t<T>;
   if (slab >= s.n_slabs[k]) return;
   const int N1 = s.N[1], N2 = s.N[2], ld = N2 + 1;
-  const int lim = N1 * ld, Wy = lim, Wz = Wy + N1;  // shared layout: plane, W_y, W_z
+  const int L1y = s.L1[1], L2y = s.L2[1];
+  const bool fold = L1y > 1 && L2y > 1;  // y passes with the plane's boundaries folded in
+  // Shared layout: plane [N1][ld], W_y [N1], W_z [N2], row mask [N1] int.
+  const int lim = N1 * ld, Wy = lim, Wz = Wy + N1;
   C2* sm = smem_c<T>();
+  int* rowmask = reinterpret_cast<int*>(sm + Wz + N2);
   const C2* tw = static_cast<const C2*>(s.twiddle);
   load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
   load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
   const C2 zero = mk<T>(T(0), T(0));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  for (int r = warp; r < N1; r += nwarps)
-    for (int c = lane; c < N2; c += 32) sm[r * ld + c] = zero;
+  const int r0 = s.row_start[k * (s.max_slabs + 1) + slab];
+  const int nrows = s.row_start[k * (s.max_slabs + 1) + slab + 1] - r0;
+  const int* rows = s.rows + r0;
+  if (fold) {
+    // Only the touched rows are zero-filled: the first y pass reads the others as zero.
+    for (int y = threadIdx.x; y < N1; y += blockDim.x) rowmask[y] = 0;
+    for (int i = warp; i < nrows; i += nwarps) {
+      const int y = rows[i];
+      if (!QGB_OK_IDX(y, N1, 68)) continue;
+      for (int c = lane; c < N2; c += 32) sm[y * ld + c] = zero;
+    }
+  } else {
+    for (int r = warp; r < N1; r += nwarps)
+      for (int c = lane; c < N2; c += 32) sm[r * ld + c] = zero;
+  }
   __syncthreads();
+  if (fold) {
+    for (int i = threadIdx.x; i < nrows; i += blockDim.x) {
+      const int y = rows[i];
+      if (QGB_OK_IDX(y, N1, 68)) rowmask[y] = 1;
+    }
+  }
 
   // Scatter this slab's coefficients (contiguous in the basis) into the plane.
   const int g0 = s.slab_start[k * (s.max_slabs + 1) + slab];
@@ -108,14 +276,18 @@ __device__ __forceinline__ void body_ifft_yz(const qgb_sphere& s, const LocalPar
   __syncthreads();
 
   // Inverse z-FFT along the rows this slab touches (row stride ld, element stride 1).
-  const int r0 = s.row_start[k * (s.max_slabs + 1) + slab];
-  const int nrows = s.row_start[k * (s.max_slabs + 1) + slab + 1] - r0;
-  fft_inverse<T>(0, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz, lim);
-  // Inverse y-FFT along all N2 columns (column stride 1, element stride ld).
-  fft_inverse<T>(0, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy, lim);
-
+  fft_inverse<T>(0, rows, nrows, ld, 1, s.L1[2], s.L2[2], Wz, lim);
   if (!QGB_OK_IDX(plane_index(s, k, b, lp.nb, slab), (long long)s.nk * lp.nb * s.max_slabs, 4)) return;
   C2* out = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
+  if (fold) {
+    // Inverse y-FFT along all N2 columns; its second pass stores the plane.
+    ypass<T, 0>(L2y, rowmask, nullptr, N2, N2, L1y, L2y, ld, Wy, lim);
+    __syncthreads();
+    ypass<T, 1>(L1y, rowmask, out, N2, N2, L1y, L2y, ld, Wy, lim);
+    return;
+  }
+  // Inverse y-FFT along all N2 columns (column stride 1, element stride ld).
+  fft_inverse<T>(0, nullptr, N2, 1, ld, L1y, L2y, Wy, lim);
   for (int r = warp; r < N1; r += nwarps)
     for (int c = lane; c < N2; c += 32) out[r * N2 + c] = sm[r * ld + c];
 }
@@ -288,12 +460,99 @@ __device__ __forceinline__ void xmid_dispatch(int L1, cplx_t<T>* sm, int p, int 
   }
 }
 
-// x-pass with asynchronous staging (FP32, N2 % 4 == 0): the slab rows are
-// copied to shared memory with cp.async (no register staging).  The middle
-// step reads V(r) from global memory (it stays in L2 across the bands), which
-// keeps shared memory at 75 KB for si64 (96^3) so that 3 CTAs fit an SM;
-// staging the V slice as well (111 KB, 2 CTAs) made the local apply 6%
-// slower.  Shared layout: pencils [N0][ldx = N2 + 2] complex, W_x [N0] complex.
+// x-pass first inverse pass straight from the slab planes: item (column c,
+// sub) is the L2-point DFT over x = sub + j * L1 (natural order), read from the
+// plane of slab xs[x] (zero where no slab), times the pass-1 twiddles, stored
+// at the same shared rows.  Covers every row, so no zero fill is needed.
+template <typename T, int R>
+__device__ __forceinline__ void xpass_first_R(const cplx_t<T>* __restrict__ base, size_t plane, const int* xs,
+                                              int nz, int L1, int ld, int Wx, int lim) {
+  cplx_t<T>* sm = smem_c<T>();
+  const int nitems = nz * L1;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int sub = it / nz;
+    const int c = it - sub * nz;
+    T re[R], im[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int sl = xs[sub + j * L1];
+      cplx_t<T> v = mk<T>(T(0), T(0));
+      if (sl >= 0) v = base[static_cast<size_t>(sl) * plane + c];
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    Codelet<R, +1>::run(re, im);
+#pragma unroll
+    for (int j = 1; j < R; ++j) {
+      const cplx_t<T> w = sm[Wx + sub * R + j];
+      const T xr = re[j] * w.x - im[j] * w.y;
+      const T xi = re[j] * w.y + im[j] * w.x;
+      re[j] = xr;
+      im[j] = xi;
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int off = (sub + j * L1) * ld + c;
+      if (!QGB_OK_IDX(off, lim, 61)) return;
+      sm[off] = mk<T>(re[j], im[j]);
+    }
+  }
+}
+
+// x-pass last forward pass straight to the slab planes: the L2-point DFT over
+// the shared rows sub + j * L1 gives natural x = sub + j * L1; only the rows of
+// a slab (xs[x] >= 0) are stored.
+template <typename T, int R>
+__device__ __forceinline__ void xpass_last_R(cplx_t<T>* __restrict__ base, size_t plane, const int* xs, int nz,
+                                             int L1, int ld, int lim) {
+  cplx_t<T>* sm = smem_c<T>();
+  const int nitems = nz * L1;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int sub = it / nz;
+    const int c = it - sub * nz;
+    T re[R], im[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int off = (sub + j * L1) * ld + c;
+      if (!QGB_OK_IDX(off, lim, 62)) return;
+      const cplx_t<T> v = sm[off];
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    Codelet<R, -1>::run(re, im);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int sl = xs[sub + j * L1];
+      if (sl >= 0) base[static_cast<size_t>(sl) * plane + c] = mk<T>(re[j], im[j]);
+    }
+  }
+}
+
+template <typename T, bool FIRST>
+__device__ __forceinline__ void xpass_outer(int R, cplx_t<T>* base, size_t plane, const int* xs, int nz, int L1,
+                                            int ld, int Wx, int lim) {
+#define QGB_XO(RR)                                                   \
+  case RR:                                                           \
+    if constexpr (FIRST)                                             \
+      xpass_first_R<T, RR>(base, plane, xs, nz, L1, ld, Wx, lim);    \
+    else                                                             \
+      xpass_last_R<T, RR>(base, plane, xs, nz, L1, ld, lim);         \
+    break;
+  switch (R) {
+    QGB_XO(2) QGB_XO(3) QGB_XO(4) QGB_XO(5) QGB_XO(6) QGB_XO(7) QGB_XO(8) QGB_XO(9) QGB_XO(10) QGB_XO(12)
+    QGB_XO(14) QGB_XO(15) QGB_XO(16)
+    default: break;
+  }
+#undef QGB_XO
+}
+
+// x-pass (FP32, N2 % 4 == 0, L2 > 1) with its outer passes on the slab planes:
+// the first inverse pass reads the slab rows from global memory (L2) and the
+// last forward pass stores the slab rows back, so shared memory sees each
+// element in three passes only (no zero fill, staging or write-back).  The
+// middle step reads V(r) from global memory (it stays in L2 across the bands).
+// Shared layout: pencils [N0][ld = nz + 2] complex, W_x [N0] complex, x -> slab
+// table [N0] int.  75 KB for si64 (96^3), so 3 CTAs fit an SM.
 template <typename T>
 __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const LocalParams& lp,
                                                  cplx_t<T>* __restrict__ planes, const int r1, const int b,
@@ -303,32 +562,22 @@ __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const Loca
   const int L1 = s.L1[0], L2 = s.L2[0];
   const int lim = N0 * ld, Wx = lim;
   C2* sm = smem_c<T>();
+  int* xs = reinterpret_cast<int*>(sm + Wx + N0);
   const C2* tw = static_cast<const C2*>(s.twiddle);
   load_twiddles<T>(Wx, tw + s.tw_off[0], N0);
-  const C2 zero = mk<T>(T(0), T(0));
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  for (int r = warp; r < N0; r += nwarps)
-    for (int c = lane; c < nz; c += 32) sm[r * ld + c] = zero;
+  for (int x = threadIdx.x; x < N0; x += blockDim.x) xs[x] = -1;
   __syncthreads();
-
   const int nslabs = s.n_slabs[k];
   const int* i0 = s.slab_i0 + k * s.max_slabs;
+  for (int sl = threadIdx.x; sl < nslabs; sl += blockDim.x) {
+    const int x = i0[sl];
+    if (QGB_OK_IDX(x, N0, 63)) xs[x] = sl;
+  }
+  __syncthreads();
   const size_t plane = static_cast<size_t>(N1) * N2;
   C2* base = planes + plane_index(s, k, b, lp.nb, 0) * plane + static_cast<size_t>(r1) * N2 + z0;
-  // Slab rows, columns [z0, z0 + nz) (16 B = 2 complex per copy).
-  const int cpr = nz / 2;  // copies per row
-  for (int it = threadIdx.x; it < nslabs * cpr; it += blockDim.x) {
-    const int sl = it / cpr, c = 2 * (it - sl * cpr);
-    cp_async16(sm + i0[sl] * ld + c, base + sl * plane + c);
-  }
-  cp_async_commit();
-  cp_async_wait<0>();
+  xpass_outer<T, true>(L2, base, plane, xs, nz, L1, ld, Wx, lim);
   __syncthreads();
-
-  if (L2 > 1) {
-    run_pass<T, +1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, Wx, L2, 1, lim, Wx + N0});
-    __syncthreads();
-  }
   // V[p0][r1][z0 + c] with p0 = a * L1 + j: j-stride N1 * N2.
   const T* V = static_cast<const T*>(s.V) + static_cast<size_t>(r1) * N2 + z0;
   for (int it = threadIdx.x; it < nz * L2; it += blockDim.x) {
@@ -338,15 +587,7 @@ __device__ __forceinline__ void body_xpass_async(const qgb_sphere& s, const Loca
                      static_cast<size_t>(N1) * N2, Wx, L2, a);
   }
   __syncthreads();
-  if (L2 > 1) {
-    run_pass<T, -1>(L2, Pass{nullptr, 0, nz, 1, L1, ld, L1 * ld, -1, 0, 0, lim, 0});
-    __syncthreads();
-  }
-  for (int sl = warp; sl < nslabs; sl += nwarps) {
-    C2* dst = base + sl * plane;
-    const int x = i0[sl];
-    for (int c = lane; c < nz; c += 32) dst[c] = sm[x * ld + c];
-  }
+  xpass_outer<T, false>(L2, base, plane, xs, nz, L1, ld, Wx, lim);
 }
 
 template <typename T>
@@ -367,21 +608,39 @@ __device__ __forceinline__ void body_fft_yz_gather(const qgb_sphere& s, const Lo
   C2* sm = smem_c<T>();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   if (!QGB_OK_IDX(plane_index(s, k, b, lp.nb, slab), (long long)s.nk * lp.nb * s.max_slabs, 4)) return;
-  // Stage the plane asynchronously (padded rows are 8-byte aligned only, so one
-  // element per copy), then the twiddles while the copies are in flight.
   const C2* in = planes + plane_index(s, k, b, lp.nb, slab) * (static_cast<size_t>(N1) * N2);
-  for (int r = warp; r < N1; r += nwarps)
-    for (int c = lane; c < N2; c += 32) cp_async_elem<T>(sm + r * ld + c, in + r * N2 + c);
-  cp_async_commit();
-  const C2* tw = static_cast<const C2*>(s.twiddle);
-  load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
-  load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
-  cp_async_wait<0>();
-  __syncthreads();
-
-  fft_forward<T>(0, nullptr, N2, 1, ld, s.L1[1], s.L2[1], Wy, lim);
+  const int L1y = s.L1[1], L2y = s.L2[1];
   const int r0 = s.row_start[k * (s.max_slabs + 1) + slab];
   const int nrows = s.row_start[k * (s.max_slabs + 1) + slab + 1] - r0;
+  const C2* tw = static_cast<const C2*>(s.twiddle);
+  if (L1y > 1 && L2y > 1) {
+    // The first forward y pass reads the plane from global memory; the second
+    // stores only the rows the z-FFT and the gather use.
+    int* rowmask = reinterpret_cast<int*>(sm + Wz + N2);
+    for (int y = threadIdx.x; y < N1; y += blockDim.x) rowmask[y] = 0;
+    load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
+    load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nrows; i += blockDim.x) {
+      const int y = s.rows[r0 + i];
+      if (QGB_OK_IDX(y, N1, 68)) rowmask[y] = 1;
+    }
+    ypass<T, 2>(L1y, rowmask, const_cast<C2*>(in), N2, N2, L1y, L2y, ld, Wy, lim);
+    __syncthreads();
+    ypass<T, 3>(L2y, rowmask, nullptr, N2, N2, L1y, L2y, ld, Wy, lim);
+    __syncthreads();
+  } else {
+    // Stage the plane asynchronously (padded rows are 8-byte aligned only, so one
+    // element per copy), then the twiddles while the copies are in flight.
+    for (int r = warp; r < N1; r += nwarps)
+      for (int c = lane; c < N2; c += 32) cp_async_elem<T>(sm + r * ld + c, in + r * N2 + c);
+    cp_async_commit();
+    load_twiddles<T>(Wy, tw + s.tw_off[1], N1);
+    load_twiddles<T>(Wz, tw + s.tw_off[2], N2);
+    cp_async_wait<0>();
+    __syncthreads();
+    fft_forward<T>(0, nullptr, N2, 1, ld, L1y, L2y, Wy, lim);
+  }
   fft_forward<T>(0, s.rows + r0, nrows, ld, 1, s.L1[2], s.L2[2], Wz, lim);
 
   const int g0 = s.slab_start[k * (s.max_slabs + 1) + slab];
@@ -512,7 +771,7 @@ __global__ void __launch_bounds__(kThreads) k_xpass_batched(const qgb_batch_item
   const int r1 = static_cast<int>(local % s.N[1]);
   const long long rest = local / s.N[1];
   const int b = static_cast<int>(rest % ctx.it.nb), k = static_cast<int>(rest / ctx.it.nb);
-  if (sizeof(T) == 4 && s.N[2] % 4 == 0)
+  if (sizeof(T) == 4 && s.N[2] % 4 == 0 && s.L2[0] > 1)
     body_xpass_async<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k, 0, s.N[2]);
   else
     body_xpass<T>(s, lp, static_cast<cplx_t<T>*>(ctx.it.planes), r1, b, k);
@@ -576,17 +835,17 @@ static bool codelet_size(int R) {
 
 size_t plane_smem_bytes(const qgb_sphere& s, int dtype) {
   const size_t e = elem_bytes(dtype);
-  const size_t yz = (static_cast<size_t>(s.N[1]) * (s.N[2] + 1) + s.N[1] + s.N[2]) * e;
+  const size_t yz = (static_cast<size_t>(s.N[1]) * (s.N[2] + 1) + s.N[1] + s.N[2]) * e + s.N[1] * sizeof(int);
   const size_t x = (static_cast<size_t>(s.N[0]) * (s.N[2] + 1) + s.N[0]) * e;
   return std::max(yz, x);
 }
 
 // The asynchronous x-pass: FP32 with 16-byte aligned rows of V and of the planes.
-static bool xpass_async_ok(const qgb_sphere& s, int dtype) { return dtype == QGB_F32 && s.N[2] % 4 == 0; }
+static bool xpass_async_ok(const qgb_sphere& s, int dtype) { return dtype == QGB_F32 && s.N[2] % 4 == 0 && s.L2[0] > 1; }
 
 static size_t xpass_async_smem_bytes(const qgb_sphere& s) {
-  const size_t cplx = (static_cast<size_t>(s.N[0]) * (s.N[2] + 2) + s.N[0] + 1) & ~static_cast<size_t>(1);
-  return cplx * 8;
+  const size_t cplx = static_cast<size_t>(s.N[0]) * (s.N[2] + 2) + s.N[0];
+  return cplx * 8 + static_cast<size_t>(s.N[0]) * 4;
 }
 
 int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true) {
@@ -630,12 +889,12 @@ static int launch_xpass_async(const qgb_sphere& s, const LocalParams& lp, float2
 
 template <typename T>
 static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* C, void* out,
-                        void* planes, cudaStream_t st, size_t smem) {
+                        void* planes, cudaStream_t st, size_t smem, cudaEvent_t gather_after) {
   using C2 = cplx_t<T>;
   const dim3 g1(s.max_slabs, lp.nb, s.nk);
   k_ifft_yz<T><<<g1, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(C), static_cast<C2*>(planes));
   QGB_LAUNCH_CHECK("k_ifft_yz");
-  if (sizeof(T) == 4 && s.N[2] % 4 == 0) {
+  if (sizeof(T) == 4 && xpass_async_ok(s, QGB_F32)) {
     const int rc = launch_xpass_async(s, lp, static_cast<float2*>(planes), st);
     if (rc) return rc;
   } else {
@@ -643,6 +902,7 @@ static int launch_chunk(const qgb_sphere& s, const LocalParams& lp, const void* 
     k_xpass<T><<<g2, kThreads, smem, st>>>(s, lp, static_cast<C2*>(planes));
     QGB_LAUNCH_CHECK("k_xpass");
   }
+  if (gather_after) QGB_CUDA_CHECK(cudaStreamWaitEvent(st, gather_after, 0));
   k_fft_yz_gather<T><<<g1, kThreads, smem, st>>>(s, lp, static_cast<const C2*>(C),
                                                 static_cast<C2*>(out), static_cast<const C2*>(planes));
   QGB_LAUNCH_CHECK("k_fft_yz_gather");
@@ -657,8 +917,11 @@ static int set_smem_limits(size_t smem) {
   return raise_smem_limit(k_fft_yz_gather<T>, smem);
 }
 
+// gather_after (optional): an event the gather kernels wait for, so that a
+// term written into `out` on another stream (QGB_ACCUMULATE) can be produced
+// while the inverse and x passes run.
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb,
-                    unsigned flags, void* ws, size_t ws_bytes, cudaStream_t st) {
+                    unsigned flags, void* ws, size_t ws_bytes, cudaStream_t st, cudaEvent_t gather_after = nullptr) {
   int rc = validate_sphere(s, dtype);
   if (rc) return rc;
   if (nb < 0) return fail(QGB_ERR_INVALID, "nb = %d < 0", nb);
@@ -675,8 +938,8 @@ int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, in
   if (rc) return rc;
   for (int b0 = 0; b0 < nb; b0 += chunk) {
     LocalParams lp{nb, b0, std::min(chunk, nb - b0), flags};
-    rc = (dtype == QGB_F64) ? launch_chunk<double>(*s, lp, C, out, ws, st, smem)
-                            : launch_chunk<float>(*s, lp, C, out, ws, st, smem);
+    rc = (dtype == QGB_F64) ? launch_chunk<double>(*s, lp, C, out, ws, st, smem, gather_after)
+                            : launch_chunk<float>(*s, lp, C, out, ws, st, smem, gather_after);
     if (rc) return rc;
   }
   return QGB_OK;

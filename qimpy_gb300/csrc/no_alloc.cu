@@ -20,7 +20,8 @@ namespace qgb {
 int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true);
 size_t plane_bytes_per_band(const qgb_sphere& s, int dtype);
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
-                    void* ws, size_t ws_bytes, cudaStream_t st);
+                    void* ws, size_t ws_bytes, cudaStream_t st,
+                    cudaEvent_t gather_after = nullptr);
 
 // 32 MiB per GPU that loads this library, held until the process exits.
 static constexpr size_t kStaticScratchBytes = size_t(32) << 20;

@@ -28,7 +28,8 @@ namespace qgb {
 int validate_sphere(const qgb_sphere* s, int dtype, bool need_potential = true);
 size_t plane_bytes_per_band(const qgb_sphere& s, int dtype);
 int apply_potential(const qgb_sphere* s, int dtype, const void* C, void* out, int nb, unsigned flags,
-                    void* ws, size_t ws_bytes, cudaStream_t st);
+                    void* ws, size_t ws_bytes, cudaStream_t st,
+                    cudaEvent_t gather_after = nullptr);
 
 namespace rb {
 
@@ -205,15 +206,18 @@ size_t real_local_bytes(const qgb_sphere& full, const qgb_real_map& m, int nb, i
   return L.z + L.w + L.planes;
 }
 
+// HC = KE C + V C in the real mode.  With `unpack_after` (an event on another
+// stream that writes a term into HC), the unpack waits for it and adds to HC.
 int real_local(const qgb_sphere* full, const qgb_real_map* m, int dtype, const void* C, void* HC, int nb, void* ws,
-               size_t ws_bytes, cudaStream_t st) {
+               size_t ws_bytes, cudaStream_t st, cudaEvent_t unpack_after) {
   const RealLayout L = real_layout(*full, *m, nb, 0, dtype);
   if (ws_bytes < L.z + L.w + L.planes) return fail(QGB_ERR_WORKSPACE, "real local workspace too small");
   char* w = static_cast<char*>(ws);
   int rc;
   if ((rc = real_pack(dtype, m, C, nb, w, st))) return rc;
   if ((rc = apply_potential(full, dtype, w, w + L.z, (nb + 1) / 2, 0u, w + L.z + L.w, L.planes, st))) return rc;
-  return real_unpack(dtype, m, w + L.z, C, nb, HC, QGB_ADD_KE, st);
+  if (unpack_after) QGB_CUDA_CHECK(cudaStreamWaitEvent(st, unpack_after, 0));
+  return real_unpack(dtype, m, w + L.z, C, nb, HC, QGB_ADD_KE | (unpack_after ? QGB_ACCUMULATE : 0u), st);
 }
 
 }  // namespace qgb

@@ -49,6 +49,7 @@ struct GemmArgs {
   float2* hc;              // EPI_ADD_HC: complex64 [batch][nb][hc_ld], += D
   long long hc_batch_stride;
   int hc_ld, nb;
+  int hc_store;            // EPI_ADD_HC: 1 = store D instead of adding it
   int* err;                // device error word (0 = ok)
   unsigned long long timeout_ns;  // limit of each pipeline wait (kTimeoutNs)
   int skip_loads;          // test aid: the producer issues no copies, so the MMA wait runs out
@@ -305,7 +306,10 @@ __global__ void __launch_bounds__(kThreads)
         // writes through one pointer could alias, which would serialise 32
         // memory round trips per thread.
         float2 o[32];
-        if (row_ok) {
+        if (args.hc_store) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) o[i] = make_float2(0.f, 0.f);
+        } else if (row_ok) {
 #pragma unroll
           for (int i = 0; i < 32; ++i) {
             const int b = n_tile * HB + c0 + i;
@@ -690,7 +694,8 @@ size_t nonlocal_tc_workspace_bytes(int nk, int P, int nb, int n_tot) {
 }
 
 // phases: 1 = steps 1-3 (everything that depends only on C), 2 = step 4 (the
-// accumulation into HC), 3 = both.  Phase 1 may run beside the local potential.
+// accumulation into HC), 3 = both; with 4 added, step 4 stores beta (D proj)
+// into HC instead of adding it.  Phase 1 may run beside the local potential.
 template <int BN>
 static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int pa, const void* C, void* HC,
                             void* projT, int nk, int nb, int n_tot, const NlWorkspace& W, unsigned char* ws,
@@ -757,6 +762,7 @@ static int nonlocal_tc_impl(const void* split, const void* D, int n_atoms, int p
   g2.hc_batch_stride = static_cast<long long>(nb) * n_tot;
   g2.hc_ld = n_tot;
   g2.nb = nb;
+  g2.hc_store = (phases & 4) ? 1 : 0;
   g2.err = err;
   return launch<BN, kStages<BN>, EPI_ADD_HC>(
       Operand{t_hi, t_lo, n_tot, BL.ldT, static_cast<long long>(n_tot) * BL.ldT},

@@ -87,11 +87,16 @@ def test_real_hamiltonian_mixed_matches_oracle(name, nb, hermitian):
         oh.real_symmetrize(C, half.iG[0], p.grid_shape)
     want, want_proj = _oracle(p, half, beta, C)
     split = ops.beta_split(torch.from_numpy(beta).to(DEV, torch.complex64))
+    # The nonlocal term is stored into HC beside the local potential, whose
+    # unpack then adds to it: every entry is written (NaN before the call).
+    out = torch.full(C.shape, float("nan"), dtype=torch.complex64, device=DEV)
     HC, projT = ops.hamiltonian_real_mixed(rb, torch.from_numpy(C).to(DEV, torch.complex64), split,
-                                           torch.from_numpy(p.D_atom).to(DEV, torch.complex64))
+                                           torch.from_numpy(p.D_atom).to(DEV, torch.complex64), out=out)
     torch.cuda.synchronize()
     assert int(ops.device_error_word(DEV).item()) == 0
-    assert _rel(HC.cpu().numpy().astype(np.complex128), want) <= TOL[torch.complex64]
+    HCn = HC.cpu().numpy().astype(np.complex128)
+    assert np.isfinite(HCn).all() and not HCn[0, :, int(half.n[0]):].any()
+    assert _rel(HCn, want) <= TOL[torch.complex64]
     pr = projT.cpu().numpy().astype(np.complex128).transpose(0, 2, 1)
     assert _rel(pr, want_proj) <= TOL[torch.complex64] and not pr.imag.any()
 
