@@ -260,12 +260,15 @@ def roofline_counts(p, b, tables, nb_tile: int, real_bytes: int):
     return dict(flops_loc=flops_loc, flops_nl=flops_nl, bytes_loc=bytes_loc, bytes_nl=bytes_nl)
 
 
-# DRAM bytes (read + write) per 32-band si64 block, from one ncu capture of the
+# DRAM bytes (read + write) per 32-band si64 block, from ncu captures of the
 # mixed form (`--set full`, default cache control: caches flushed before every
 # kernel, so planes one kernel writes and the next reads count as DRAM traffic
-# although they stay in L2 in a timed run).  A recorded constant of that
-# capture, not measured by this run.
-NCU_DRAM_BYTES_PER_BLOCK = {"local": 295.0e6, "nonlocal": 195.9e6}
+# although they stay in L2 in a timed run).  Recorded constants of those
+# captures, not measured by this run: the local potential's three kernels as
+# they are now (292.9 MB), the nonlocal chain as captured before its
+# back-projection stored instead of accumulating (195.9 MB; storing skips one
+# 9.5 MB read of HC).
+NCU_DRAM_BYTES_PER_BLOCK = {"local": 292.9e6, "nonlocal": 195.9e6}
 
 # Throughput of the reference's own torch-CPU Electrons.hamiltonian over the
 # oracle port on the same inputs and host (si64, every host thread of an
