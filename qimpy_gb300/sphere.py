@@ -213,9 +213,11 @@ class DeviceSphere:
         self._V = self.permute_real(V)
         self.struct.V = self._V.data_ptr()
 
-    #: Default bound on the slab planes of one band chunk: small enough that the
-    #: planes written by k_ifft_yz are still in L2 (126 MB) for k_xpass and
-    #: k_fft_yz_gather.  The autotuner may override it per sphere.
+    #: Default bound on the slab planes of one band chunk (1 GB: a whole block of
+    #: bands in one chunk).  A budget that kept a chunk's planes inside the 126 MB
+    #: L2 measured slower on si64 than one chunk per 32-band block (whose 97 MB
+    #: of planes mostly stay in L2).  Callers may lower it per sphere, e.g. to a
+    #: 32-band FFT block when one call covers many more bands.
     plane_budget_bytes = 1 << 30
 
     def workspace_bytes(self, nb: int, budget: int | None = None) -> int:

@@ -44,6 +44,11 @@ int main(void) {
   rc = qgb_collect_density(&s, QGB_F64, NULL, 1, NULL, NULL, 0u, NULL, 0, NULL);
   expect(rc == QGB_ERR_INVALID, "collect_density rejects a bad factorisation");
   rc = qgb_apply_nonlocal_tc_phase(NULL, NULL, 1, 4, NULL, NULL, NULL, 1, 1, 1, NULL, 0, NULL, 5, NULL);
-  expect(rc == QGB_ERR_INVALID, "nonlocal phase must be 1, 2 or 3");
+  expect(rc == QGB_ERR_INVALID, "the store flag (4) needs phase 2");
+  rc = qgb_apply_nonlocal_tc_phase(NULL, NULL, 1, 4, NULL, NULL, NULL, 1, 1, 1, NULL, 0, NULL, 8, NULL);
+  expect(rc == QGB_ERR_INVALID, "nonlocal phases are 1, 2 or 3, plus 4 with 2");
+  rc = qgb_apply_nonlocal_tc_phase(NULL, NULL, 1, 4, NULL, NULL, NULL, 1, 1, 1, NULL, 0, NULL, 6, NULL);
+  expect(rc == QGB_ERR_INVALID && strstr(qgb_last_error(), "NULL") != NULL,
+         "a valid store phase still rejects NULL pointers");
   return failures ? 1 : 0;
 }
