@@ -952,8 +952,8 @@ size_t sphere_smem_bytes(const qgb_sphere& s, int dtype) {
 }
 
 // The y/z kernels get the y/z-phase shared memory and the x kernel its own
-// (larger for the asynchronous FP32 x-pass, which also stages V): giving all
-// three the largest size would cost the y/z kernels a CTA per SM.
+// (the largest sphere of the batch sets each): giving all three the largest
+// size would cost the kernels of the smaller phase CTAs per SM.
 template <typename T>
 static int launch_batched(const qgb_batch_item* items, const int* slab_item, const long long* slab_starts,
                           const int* row_item, const long long* row_starts, long long n_slab, long long n_row,
