@@ -182,7 +182,17 @@ struct GramPlan {
 };
 static GramPlan gram_plan(int nk, int M, int N, int K, size_t elem) {
   GramPlan p;
+  // Skinny tiles for skinny outputs; otherwise the tile shape that pads the
+  // output least (M = 256 projectors x N = 160 bands: 128 x 32 tiles cover it
+  // exactly, 64 x 64 tiles would compute 20% more), the square 64 x 64 tile
+  // on ties, as its loads feed the most multiply-adds.
+  auto padded = [M, N](int shape) {
+    const long long bi = 4 * shape, bj = 4 * (256 / shape);
+    return ((M + bi - 1) / bi) * bi * ((N + bj - 1) / bj) * bj;
+  };
   p.shape = (N <= 32 && M > 32) ? 32 : ((M <= 32 && N > 32) ? 8 : 16);
+  for (const int shape : {16, 32, 8})
+    if (padded(shape) < padded(p.shape)) p.shape = shape;
   const int bi = 4 * p.shape, bj = 4 * (256 / p.shape);
   p.ti = (M + bi - 1) / bi;
   p.tj = (N + bj - 1) / bj;
