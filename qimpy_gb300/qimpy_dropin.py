@@ -20,11 +20,17 @@ replaces, with calls through the C ABI of ``libqimpy_gb300.so``:
 The eigensolvers themselves (``Davidson``, ``CheFSI``), the remaining
 Wavefunction arithmetic and the preconditioner stay QimPy's own code.
 
-Scope: one spin channel, no spinors, complex wavefunctions on the full basis of
-one process (no basis division), norm-conserving pseudopotentials (overlap =
-identity), no kinetic-energy-density or DFT+U terms.  Anything else raises
-``NotImplementedError``: the binding has no path other than the C ABI, and
-every call needs CUDA tensors (QimPy's ``rc.device`` a CUDA device).
+Scope: one spin channel, no spinors, the full basis of one process (no basis
+division), norm-conserving pseudopotentials (overlap = identity), no
+kinetic-energy-density or DFT+U terms.  Wavefunctions may be complex, or real
+at the Gamma point (``basis.real_wavefunctions``, the half-mesh basis of
+qimpy/dft/electrons/_basis_real.py): there ``Electrons.hamiltonian`` runs
+through ``qgb_hamiltonian_real`` (two real bands per complex transform on the
+full Gamma sphere) and the overlaps through ``qgb_dot_real`` (the G-weighted
+real products of _wavefunction_dot.py:55-88); ``apply_ke``, ``apply_potential``
+and ``collect_density`` are replaced for complex wavefunctions only.  Anything
+else raises ``NotImplementedError``: the binding has no path other than the C
+ABI, and every call needs CUDA tensors (QimPy's ``rc.device`` a CUDA device).
 ``uninstall()`` restores the original attributes.
 """
 from __future__ import annotations
@@ -33,6 +39,8 @@ import numpy as np
 import torch
 
 from . import linalg, ops
+from . import workloads as wl
+from .real_basis import DeviceRealBasis
 from .sphere import DeviceSphere, build_tables
 
 #: (owner, attribute name) -> the attribute install() replaced
@@ -54,7 +62,6 @@ def _coeff3(C) -> torch.Tensor:
     c = C.coeff
     _require(c.dim() == 5 and c.shape[0] == 1 and c.shape[3] == 1,
              f"wavefunction shape {tuple(c.shape)} (one spin channel, no spinors)")
-    _require(not C.basis.real_wavefunctions, "real wavefunctions")
     _require(c.shape[-1] == C.basis.n_tot, "wavefunction on part of the basis")
     _single_process(C.basis)
     return c[0, :, :, 0, :].resolve_conj().resolve_neg().contiguous()
@@ -75,6 +82,28 @@ def _sphere(basis, dtype: torch.dtype, device: torch.device) -> DeviceSphere:
         ds = cache[key] = DeviceSphere(tables, ke, device, dtype)
         ds._qgb_V_key = None
     return ds
+
+
+def _real_basis(basis, dtype: torch.dtype, device: torch.device) -> DeviceRealBasis:
+    """The real-wavefunction tables of a Gamma-point `basis` on `device`: its
+    half-mesh basis (the reference's own fft_index, iG and kinetic energies)
+    against the full Gamma sphere of the same lattice, cutoff and grid, built
+    once per basis, dtype and device."""
+    cache = basis.__dict__.setdefault("_qgb_real", {})
+    key = (dtype, str(device))
+    rb = cache.get(key)
+    if rb is None:
+        k = basis.k.detach().cpu().numpy()
+        _require(k.shape[0] == 1 and not k.any(), "real wavefunctions away from the Gamma point")
+        shape = tuple(int(x) for x in basis.grid.shape)
+        half = wl.BasisLayout(grid_shape=shape, n=basis.n.cpu().numpy().astype(np.int64), n_tot=int(basis.n_tot),
+                              fft_index=basis.fft_index.cpu().numpy().astype(np.int64),
+                              iG=basis.iG.cpu().numpy().astype(np.int64), ke=basis.get_ke().detach().cpu().numpy())
+        full = wl.make_basis(basis.lattice.Gbasis.detach().cpu().numpy(), np.zeros((1, 3)), float(basis.ke_cutoff),
+                             shape)
+        rb = cache[key] = DeviceRealBasis(half, full, device, dtype)
+        rb._qgb_V_key = None
+    return rb
 
 
 def _set_potential(ds: DeviceSphere, basis, V) -> None:
@@ -138,6 +167,7 @@ def _nonlocal(basis, dtype: torch.dtype, device: torch.device):
 
 def apply_ke(self, C):
     """Basis.apply_ke (_basis_ops.py:29-36) through qgb_apply_ke."""
+    _require(not self.real_wavefunctions, "apply_ke of real wavefunctions")
     C3 = _coeff3(C)
     ds = _sphere(self, C3.dtype, C3.device)
     return _wavefunction(C, ops.apply_ke(ds, C3))
@@ -145,6 +175,7 @@ def apply_ke(self, C):
 
 def apply_potential(self, V, C):
     """Basis.apply_potential (_basis_ops.py:39-113) through qgb_apply_potential."""
+    _require(not self.real_wavefunctions, "apply_potential of real wavefunctions")
     C3 = _coeff3(C)
     ds = _sphere(self, C3.dtype, C3.device)
     _set_potential(ds, self, V)
@@ -157,6 +188,7 @@ def collect_density(self, C, f: torch.Tensor, need_Mvec: bool):
     from qimpy.grid import FieldR
 
     _require(not need_Mvec, "magnetization vector (spinors)")
+    _require(not self.real_wavefunctions, "collect_density of real wavefunctions")
     C3 = _coeff3(C)
     assert tuple(f.shape) == tuple(C.coeff.shape[:3])
     ds = _sphere(self, C3.dtype, C3.device)
@@ -171,9 +203,14 @@ def hamiltonian(self, C):
     _require(not self.xc.plus_U, "DFT+U")
     basis = C.basis
     C3 = _coeff3(C)
+    beta, D = _nonlocal(basis, C3.dtype, C3.device)
+    if basis.real_wavefunctions:
+        rb = _real_basis(basis, C3.dtype, C3.device)
+        _set_potential(rb, basis, self.n_tilde.grad)
+        HC, _ = ops.hamiltonian_real(rb, C3, beta, D)
+        return _wavefunction(C, HC)
     ds = _sphere(basis, C3.dtype, C3.device)
     _set_potential(ds, basis, self.n_tilde.grad)
-    beta, D = _nonlocal(basis, C3.dtype, C3.device)
     HC, _ = ops.hamiltonian(ds, C3, beta, D)
     return _wavefunction(C, HC)
 
@@ -199,7 +236,10 @@ def dot(self, other):
     assert self.basis is other.basis
     X, Y = _coeff3(self), _coeff3(other)
     _require(X.dtype == Y.dtype, f"operands of dtypes {X.dtype} and {Y.dtype}")
-    out = ops.dot(X, Y)
+    if self.basis.real_wavefunctions:
+        out = ops.dot_real(X, Y, _real_basis(self.basis, X.dtype, X.device).weight)
+    else:
+        out = ops.dot(X, Y)
     return _Ready(out[None] if X.dtype == torch.complex128 else out[None].to(torch.complex64))
 
 

@@ -4,8 +4,9 @@ Test infrastructure (``tests/test_dropin_cpu.py`` runs this file in a child
 process, where the reference source is present).  The unmodified reference is
 imported as ``tests/golden/make_golden.py`` does and given the same seeded
 problem as the goldens: V(r), the projectors and D injected, the start vectors
-orthonormalised.  ``install()`` then replaces Basis.apply_ke/apply_potential/
-collect_density, Electrons.hamiltonian, Wavefunction.dot/^/dot_O/matmul/@ and the eigensolvers'
+orthonormalised (a ``real_<name>`` case runs the reference's real-wavefunction
+mode on the half-mesh basis).  ``install()`` then replaces Basis.apply_ke/
+apply_potential/collect_density, Electrons.hamiltonian, Wavefunction.dot/^/dot_O/matmul/@ and the eigensolvers'
 eighg, and ``electrons.diagonalize()`` (the reference's Davidson,
 qimpy/dft/electrons/_davidson.py:141-235) runs to convergence through them.
 
@@ -56,6 +57,23 @@ class OracleSphere:
         self.V = V_r.detach().cpu().numpy().astype(np.float64)
 
 
+class OracleRealBasis:
+    """Stands in for DeviceRealBasis: the half-mesh basis, its overlap weights
+    and V(r) in natural order."""
+
+    def __init__(self, half, full, device, dtype):
+        self.half = half
+        n = int(half.n[0])
+        self.weight_np = oh.real_gweight(half.iG[0], n, int(half.n_tot))
+        import torch
+
+        self.weight = torch.from_numpy(self.weight_np)
+        self.V = None
+
+    def set_potential(self, V_r):
+        self.V = V_r.detach().cpu().numpy().astype(np.float64)
+
+
 def oracle_tables(fft_index, n, shape):
     return types.SimpleNamespace(fft_index=np.asarray(fft_index), n=np.asarray(n), shape=tuple(shape))
 
@@ -93,6 +111,19 @@ def make_oracle_ops(torch):
         def collect_density(ds, C, prefac):
             CALLS["collect_density"] += 1
             return t(oh.collect_density(ds.fft_index, ds.shape, C.numpy(), prefac.numpy()))
+
+        @staticmethod
+        def hamiltonian_real(rb, C, beta, D_blocks):
+            CALLS["hamiltonian_real"] += 1
+            h = rb.half
+            HC = oh.hamiltonian_real(h.ke, rb.V, h.fft_index, h.n, h.iG, beta.numpy(), _dense_D(D_blocks.numpy()),
+                                     C.numpy(), rb.weight_np)
+            return t(HC), None
+
+        @staticmethod
+        def dot_real(X, Y, weight):
+            CALLS["dot_real"] += 1
+            return t(od.dot_real(X.numpy(), Y.numpy(), weight.numpy()))
 
         @staticmethod
         def dot(X, Y):
@@ -166,6 +197,35 @@ def run(qimpy, name: str) -> dict:
     return out
 
 
+def run_real(qimpy, name: str) -> dict:
+    """Real (Gamma-point) wavefunctions: the reference's own H.psi and Davidson
+    on the half-mesh basis, as the real-mode goldens were made."""
+    import torch
+    from qimpy.dft.electrons import Davidson, Wavefunction
+
+    golden = np.load(os.path.join(HERE, "golden", f"real_{name}.npz"))
+    prob = wl.get(name)
+    mine = wl.make_basis(prob.Gbasis, prob.k, prob.ke_cutoff, prob.grid_shape, real=True)
+    system = mg.build_system(qimpy, prob, None, real=True)
+    el = mg.inject(qimpy, system, prob, wl.make_projectors(prob, mine))
+    basis = el.basis
+    assert basis.real_wavefunctions
+    C0s = golden["C0"]
+    out = {}
+    CALLS.clear()
+    C = Wavefunction(basis, coeff=torch.from_numpy(C0s[None, :, :, None, :]).clone())
+    HC = el.hamiltonian(C).coeff[0, :, :, 0, :].numpy()
+    out["hpsi_rel_err"] = float(np.abs(HC - golden["hpsi"]).max() / np.abs(golden["hpsi"]).max())
+    CALLS.clear()
+    el.C = Wavefunction(basis, coeff=torch.from_numpy(C0s[None, :, :, None, :]).clone()).orthonormalize()
+    el.deig_max = np.inf
+    solver = Davidson(electrons=el, n_iterations=200, eig_threshold=float(golden["eig_threshold"]))
+    solver()
+    out.update(eig_err=float(np.abs(el.eig[0].numpy() - golden["eig"]).max()), iterations=int(solver._i_iter),
+               golden_iterations=int(golden["davidson_iterations"]), calls=dict(CALLS))
+    return out
+
+
 def main() -> None:
     ref_src = sys.argv[1]
     names = sys.argv[2:] or ["tiny_fcc"]
@@ -175,8 +235,14 @@ def main() -> None:
     ops_, linalg_ = make_oracle_ops(torch)
     dropin.ops, dropin.linalg = ops_, linalg_
     dropin.DeviceSphere, dropin.build_tables = OracleSphere, oracle_tables
+    dropin.DeviceRealBasis = OracleRealBasis
     dropin.install()
-    out = {name: run(qimpy, name) for name in names}
+    out = {}
+    for name in names:
+        if name.startswith("real_"):
+            out[name] = run_real(qimpy, name[len("real_"):])
+        else:
+            out[name] = run(qimpy, name)
     dropin.uninstall()
     from qimpy.dft import electrons
 

@@ -172,3 +172,38 @@ def test_dropin_collect_density(monkeypatch):
     assert _rel(rho.data[0].cpu().numpy(), want) <= 1e-12
     with pytest.raises(NotImplementedError, match="magnetization"):
         dropin.collect_density(basis, C, f, True)
+
+
+def test_dropin_real_wavefunctions():
+    """Real (Gamma-point) wavefunctions on the half-mesh basis: hamiltonian
+    through qgb_hamiltonian_real and the weighted real overlaps through
+    qgb_dot_real, against the oracle's real-mode H.psi and overlap (1e-12)."""
+    p = wl.get("tiny_gamma")
+    half = wl.make_basis(p.Gbasis, p.k, p.ke_cutoff, p.grid_shape, real=True)
+    beta = wl.make_projectors(p, half)
+    ions = _Ions()
+    basis = _Basis(p, half, ions)
+    basis.real_wavefunctions = True
+    basis.iG = torch.from_numpy(half.iG)
+    basis.k = torch.zeros((1, 3), dtype=torch.float64)
+    basis.ke_cutoff = p.ke_cutoff
+    basis.lattice = type("Lattice", (), {"Gbasis": torch.from_numpy(np.asarray(p.Gbasis))})()
+    ions.beta = _Wavefunction(basis, coeff=torch.from_numpy(beta)[None, :, :, None, :].to(DEV))
+    ions.D_all = torch.from_numpy(p.D_all()).to(DEV, torch.complex128)
+    ions.beta_version = 0
+    ions.n_projectors = beta.shape[1]
+    C0 = wl.make_wavefunctions(p, half, 5)
+    oh.constrain(C0, half.n)
+    oh.real_symmetrize(C0, half.iG[0], p.grid_shape)
+    C = _Wavefunction(basis, coeff=torch.from_numpy(C0)[None, :, :, None, :].to(DEV))
+    el = _Electrons(_FieldH(p.V_r))
+    gw = oh.real_gweight(half.iG[0], int(half.n[0]), half.n_tot)
+    want = oh.hamiltonian_real(half.ke, p.V_r, half.fft_index, half.n, half.iG, beta, p.D_all(), C0, gw)
+    HC = dropin.hamiltonian(el, C)
+    assert _rel(HC.coeff[0, :, :, 0, :].cpu().numpy(), want) <= 1e-12
+    O = dropin.dot(C, HC).wait()
+    Ow = od.dot_real(C0, want, gw)
+    assert O.dtype == torch.complex128 and not O.imag.any()
+    assert _rel(O[0].cpu().numpy(), Ow) <= 1e-12
+    with pytest.raises(NotImplementedError, match="real wavefunctions"):
+        dropin.apply_ke(basis, C)
