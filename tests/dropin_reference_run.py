@@ -5,7 +5,7 @@ process, where the reference source is present).  The unmodified reference is
 imported as ``tests/golden/make_golden.py`` does and given the same seeded
 problem as the goldens: V(r), the projectors and D injected, the start vectors
 orthonormalised (a ``real_<name>`` case runs the reference's real-wavefunction
-mode on the half-mesh basis).  ``install()`` then replaces Basis.apply_ke/
+mode on the half-mesh basis, a ``chefsi_<name>`` case its CheFSI eigensolver).  ``install()`` then replaces Basis.apply_ke/
 apply_potential/collect_density, Electrons.hamiltonian, Wavefunction.dot/^/dot_O/matmul/@ and the eigensolvers'
 eighg, and ``electrons.diagonalize()`` (the reference's Davidson,
 qimpy/dft/electrons/_davidson.py:141-235) runs to convergence through them.
@@ -226,6 +226,28 @@ def run_real(qimpy, name: str) -> dict:
     return out
 
 
+def run_chefsi(qimpy, name: str) -> dict:
+    """The reference's own CheFSI (qimpy/dft/electrons/_chefsi.py:72-176, its
+    Davidson warm-up included) from the goldens' start vectors."""
+    import torch
+    from qimpy.dft.electrons import CheFSI, Wavefunction
+
+    golden = np.load(os.path.join(HERE, "golden", f"chefsi_{name}.npz"))
+    cfg = mg.CHEFSI_CASES[name]
+    prob = wl.get(name)
+    mine = wl.make_basis(prob.Gbasis, prob.k, prob.ke_cutoff, prob.grid_shape)
+    system = mg.build_system(qimpy, prob, None)
+    el = mg.inject(qimpy, system, prob, wl.make_projectors(prob, mine))
+    C0 = wl.make_wavefunctions(prob, mine, prob.n_bands + prob.n_bands_extra)
+    CALLS.clear()
+    el.C = Wavefunction(el.basis, coeff=torch.from_numpy(C0[None, :, :, None, :]).clone()).orthonormalize()
+    el.deig_max = np.inf
+    solver = CheFSI(electrons=el, **cfg)
+    solver()
+    return dict(eig_err=float(np.abs(el.eig[0].numpy() - golden["eig"]).max()), iterations=int(solver._i_iter),
+                golden_iterations=int(golden["iterations"]), calls=dict(CALLS))
+
+
 def main() -> None:
     ref_src = sys.argv[1]
     names = sys.argv[2:] or ["tiny_fcc"]
@@ -241,6 +263,8 @@ def main() -> None:
     for name in names:
         if name.startswith("real_"):
             out[name] = run_real(qimpy, name[len("real_"):])
+        elif name.startswith("chefsi_"):
+            out[name] = run_chefsi(qimpy, name[len("chefsi_"):])
         else:
             out[name] = run(qimpy, name)
     dropin.uninstall()

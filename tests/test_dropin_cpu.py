@@ -1,9 +1,9 @@
 """The drop-in binding (qimpy_gb300.qimpy_dropin) against the reference's own classes.
 
 ``tests/dropin_reference_run.py`` imports the unmodified reference, installs the
-binding and runs the reference's own Davidson (qimpy/dft/electrons/_davidson.py:141-235)
-and _hamiltonian (_hamiltonian.py:7-29) through it, complex and with real
-Gamma-point wavefunctions (_basis_real.py); this host has no GPU, so the
+binding and runs the reference's own Davidson (qimpy/dft/electrons/_davidson.py:141-235),
+CheFSI (_chefsi.py:72-176) and _hamiltonian (_hamiltonian.py:7-29) through it,
+complex and with real Gamma-point wavefunctions (_basis_real.py); this host has no GPU, so the
 binding's device layer is the oracle there (the C ABI's agreement with the
 oracle is the GPU parity tests' job).  Bar: eigenvalues within 1e-10 Ha of the
 reference's own golden eigenvalues with the same iteration count, H.psi within
@@ -28,8 +28,8 @@ REF_SRC = os.environ.get("QIMPY_REFERENCE_SRC", "/root/reference/src")
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF_SRC, "qimpy")), reason="reference source not present")
 def test_reference_davidson_through_dropin():
     proc = subprocess.run([sys.executable, os.path.join(HERE, "dropin_reference_run.py"), REF_SRC,
-                           "tiny_fcc", "tiny_ortho", "si2", "real_tiny_gamma"], capture_output=True, text=True,
-                          timeout=600)
+                           "tiny_fcc", "tiny_ortho", "si2", "real_tiny_gamma", "chefsi_tiny_fcc",
+                           "chefsi_tiny_ortho"], capture_output=True, text=True, timeout=600)
     assert proc.returncode == 0, proc.stderr[-3000:]
     res = json.loads(proc.stdout.strip().splitlines()[-1])
     assert res.pop("restored") is True
