@@ -109,3 +109,75 @@ def test_unsupported_layouts_raise():
     out = dropin._coeff3(ok)
     assert not out.is_conj() and out.is_contiguous() and tuple(out.shape) == (1, 2, 8)
     assert np.array_equal(out.numpy(), np.conj((np.arange(16) * (1 + 1j)).reshape(1, 2, 8)))
+
+
+def test_dropin_caches_follow_the_reference_objects(monkeypatch):
+    """The binding converts V(r) again only when the potential changed (a new
+    field or an in-place update), and re-extracts beta and the D blocks when
+    the ions' beta_version moves; everything else is reused."""
+    calls = {"set_potential": 0, "hamiltonian": []}
+
+    class FakeSphere:
+        def __init__(self, tables, ke, device, dtype):
+            pass
+
+        def set_potential(self, V_r):
+            calls["set_potential"] += 1
+
+    class FakeOps:
+        @staticmethod
+        def hamiltonian(ds, C, beta, D):
+            calls["hamiltonian"].append((beta, D))
+            return C.clone(), None
+
+    monkeypatch.setattr(dropin, "DeviceSphere", FakeSphere)
+    monkeypatch.setattr(dropin, "build_tables", lambda fft_index, n, shape: None)
+    monkeypatch.setattr(dropin, "ops", FakeOps)
+
+    class Field:
+        def __init__(self, data):
+            self.data = data
+
+        def to(self, grid):
+            return self
+
+        def __invert__(self):
+            return Field(self.data)
+
+    class WF:
+        def __init__(self, basis, *, coeff, band_division=None):
+            self.basis, self.coeff, self.band_division = basis, coeff, band_division
+
+    basis = type("Basis", (), {})()
+    basis.fft_index, basis.n, basis.n_tot = torch.zeros((1, 4), dtype=torch.int64), torch.tensor([4]), 4
+    basis.grid = type("Grid", (), {"shape": (2, 2, 2)})()
+    basis.real_wavefunctions, basis.division = False, None
+    basis.get_ke = lambda: torch.zeros((1, 4), dtype=torch.float64)
+    ions = type("Ions", (), {})()
+    basis.ions = ions
+    D1 = torch.eye(2, dtype=torch.complex128)
+    ions.beta = WF(basis, coeff=torch.ones((1, 1, 2, 1, 4), dtype=torch.complex128))
+    ions.D_all, ions.beta_version, ions.n_projectors = D1, 0, 2
+    el = type("El", (), {})()
+    el.xc = type("Xc", (), {"need_tau": False, "plus_U": None})()
+    el.n_tilde = type("NT", (), {})()
+    el.n_tilde.grad = Field(torch.zeros((1, 2, 2, 2), dtype=torch.float64))
+    C = WF(basis, coeff=torch.ones((1, 1, 3, 1, 4), dtype=torch.complex128))
+
+    dropin.hamiltonian(el, C)
+    dropin.hamiltonian(el, C)
+    assert calls["set_potential"] == 1  # same field, unchanged
+    el.n_tilde.grad.data.add_(1.0)  # in-place update
+    dropin.hamiltonian(el, C)
+    assert calls["set_potential"] == 2
+    el.n_tilde.grad = Field(torch.zeros((1, 2, 2, 2), dtype=torch.float64))  # a new field
+    dropin.hamiltonian(el, C)
+    assert calls["set_potential"] == 3
+    b0, d0 = calls["hamiltonian"][0]
+    assert calls["hamiltonian"][3][0] is b0 and calls["hamiltonian"][3][1] is d0  # reused
+    assert tuple(d0.shape) == (2, 1, 1)  # diagonal D: one projector per block
+    ions.D_all = torch.tensor([[1.0, 0.5], [0.5, 2.0]], dtype=torch.complex128)
+    ions.beta_version += 1
+    dropin.hamiltonian(el, C)
+    b1, d1 = calls["hamiltonian"][4]
+    assert b1 is not b0 and tuple(d1.shape) == (1, 2, 2) and torch.equal(d1[0], ions.D_all)
