@@ -107,15 +107,18 @@ def _real_basis(basis, dtype: torch.dtype, device: torch.device) -> DeviceRealBa
 
 
 def _set_potential(ds: DeviceSphere, basis, V) -> None:
-    """Install V(r) = ~V on the basis grid (as _basis_ops.py:44), when V changed."""
+    """Install V(r) = ~V on the basis grid (as _basis_ops.py:44), when V changed:
+    another field object, another data tensor, or an in-place update (torch's
+    version counter).  The cache holds the field and its tensor, so that
+    neither object identity nor storage can be recycled by a new potential."""
     data = V.data
-    key = (id(V), data.data_ptr(), data._version)
-    if ds._qgb_V_key == key:
+    cached = ds._qgb_V_key
+    if cached is not None and cached[0] is V and cached[1] is data and cached[2] == data._version:
         return
     Vr = (~(V.to(basis.grid))).data
     _require(Vr.shape[0] == 1, f"{Vr.shape[0]} potential channels (one spin channel only)")
     ds.set_potential(Vr[0])
-    ds._qgb_V_key = key
+    ds._qgb_V_key = (V, data, data._version)
 
 
 def _d_blocks(D_all: torch.Tensor) -> torch.Tensor:

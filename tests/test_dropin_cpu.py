@@ -173,11 +173,14 @@ def test_dropin_caches_follow_the_reference_objects(monkeypatch):
     el.n_tilde.grad = Field(torch.zeros((1, 2, 2, 2), dtype=torch.float64))  # a new field
     dropin.hamiltonian(el, C)
     assert calls["set_potential"] == 3
+    el.n_tilde.grad.data = torch.ones((1, 2, 2, 2), dtype=torch.float64)  # a new tensor in the same field
+    dropin.hamiltonian(el, C)
+    assert calls["set_potential"] == 4
     b0, d0 = calls["hamiltonian"][0]
-    assert calls["hamiltonian"][3][0] is b0 and calls["hamiltonian"][3][1] is d0  # reused
+    assert calls["hamiltonian"][4][0] is b0 and calls["hamiltonian"][4][1] is d0  # reused
     assert tuple(d0.shape) == (2, 1, 1)  # diagonal D: one projector per block
     ions.D_all = torch.tensor([[1.0, 0.5], [0.5, 2.0]], dtype=torch.complex128)
     ions.beta_version += 1
     dropin.hamiltonian(el, C)
-    b1, d1 = calls["hamiltonian"][4]
+    b1, d1 = calls["hamiltonian"][5]
     assert b1 is not b0 and tuple(d1.shape) == (1, 2, 2) and torch.equal(d1[0], ions.D_all)
