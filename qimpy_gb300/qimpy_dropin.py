@@ -201,7 +201,8 @@ def collect_density(self, C, f: torch.Tensor, need_Mvec: bool):
 
 
 def hamiltonian(self, C):
-    """Electrons.hamiltonian (_hamiltonian.py:7-29) as one qgb_hamiltonian call."""
+    """Electrons.hamiltonian (_hamiltonian.py:7-29) as one C-ABI call:
+    qgb_hamiltonian, or qgb_hamiltonian_real for real Gamma-point wavefunctions."""
     _require(not self.xc.need_tau, "kinetic-energy-density functionals")
     _require(not self.xc.plus_U, "DFT+U")
     basis = C.basis
