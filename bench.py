@@ -274,12 +274,11 @@ def roofline_counts(p, b, tables, nb_tile: int, real_bytes: int):
 # 9.5 MB read of HC).
 NCU_DRAM_BYTES_PER_BLOCK = {"local": 292.9e6, "nonlocal": 195.9e6}
 
-# Throughput of the reference's own torch-CPU Electrons.hamiltonian over the
-# oracle port on the same inputs and host (si64, every host thread of an
-# 8-core x86 host: 1.7x at 2 bands, 1.9x at 8, 3.3x at 32); the reference
-# cannot run on the GPU host, so the CPU baseline there is the port.
 #: Reference H.psi time over the torch port's (oracle/hpsi_torch.py), si64 by
 #: band count, both on all 8 cores of one x86 host (tests/golden/time_reference_vs_port.py).
+#: The reference's source is not installed where the bench runs, so its CPU
+#: baseline is the port.  (The numpy port, oracle.hpsi, took 1.7x, 1.9x and
+#: 3.3x the reference's time at 2, 8 and 32 bands; the torch port matches it.)
 REFERENCE_OVER_PORT = {"2": 0.78, "8": 1.03, "32": 1.09, "host": "8-core x86 container, torch 2.11 CPU"}
 
 
@@ -820,8 +819,8 @@ def cpu_baseline(args, p=None, b=None, beta=None, C=None, threads=None):
     """The reference's FP64 H.psi restated with torch CPU operations (the
     reference's own library and steps: scatter, ifftn, *V, fftn, gather per
     band; nonlocal as complex matmuls) on a bounded band sample, timed on every
-    host core.  The reference itself cannot travel to the GPU host; on one x86
-    host the port runs at the reference's speed (REFERENCE_OVER_PORT)."""
+    host core.  The reference itself is not installed where the bench runs; on
+    one x86 host the port runs at the reference's speed (REFERENCE_OVER_PORT)."""
     import torch
 
     from oracle import hpsi_torch as oht

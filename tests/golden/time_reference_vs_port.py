@@ -1,7 +1,8 @@
 """Time the reference's own CPU H.psi against the oracle port on the same host.
 
-The reference is Python and cannot travel to the GPU host, where the CPU
-baseline runs the oracle port (oracle.hpsi.hamiltonian, numpy/scipy).  This
+The reference is Python and is not installed where bench.py runs, so the CPU
+baseline there runs a port (oracle/hpsi_torch.py; before it, oracle.hpsi with
+numpy/scipy).  This
 script measures, on one host, how fast the unmodified reference's
 Electrons.hamiltonian (torch CPU, every host thread) is relative to the port on
 the same inputs (every host thread), so that the baseline's ratio can be
