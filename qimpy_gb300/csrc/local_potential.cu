@@ -21,7 +21,14 @@
 //                  forward z-FFT on the touched rows, gather the slab's points,
 //                  scale by 1/N and add KE*psi.
 // Versus three full-grid passes each way this skips the empty x-planes in the
-// y/z passes and the empty z-rows in the z passes.
+// y/z passes and the empty z-rows in the z passes.  Where both factors of an
+// axis exceed 1, the passes next to global memory read or write it directly:
+// the first inverse y pass reads untouched rows as zero (no zero fill), the
+// last inverse y pass and the last forward x pass store straight to the
+// planes, and the first inverse x pass and the first forward y pass read
+// straight from them, so shared memory sees each element in the inner passes
+// only.  With QGB_ACCUMULATE the gather adds to `out` (the mixed H.psi writes
+// its nonlocal term there first, on another stream).
 #include <algorithm>
 #include <mutex>
 
