@@ -7,7 +7,6 @@ randomisation must reproduce the host restatement of the reference's seeded
 generator (davidson.randomize_selected, itself checked against the oracle on
 CPU) within 1e-13 (FP64) / 1e-6 (FP32).
 """
-import numpy as np
 import pytest
 import torch
 

@@ -9,7 +9,6 @@ already run every other test.
 """
 import ctypes as ct
 
-import numpy as np
 import pytest
 import torch
 
